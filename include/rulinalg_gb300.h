@@ -1,0 +1,193 @@
+/*
+ * rulinalg_gb300: C ABI of the GB300 (sm_103a) implementation of rulinalg's dense
+ * hot path: `Mul` for Matrix<f32>/Matrix<f64> (GEMM) and the factor-and-solve
+ * routines PartialPivLu, Cholesky and HouseholderQr with their solve/det/inverse.
+ *
+ * Conventions (all entry points):
+ *  - Matrices are row-major exactly like rulinalg's Matrix<T> (src/matrix/mod.rs:45-49)
+ *    and MatrixSlice (src/matrix/mod.rs:58-64): element (i, j) at ptr[i * ld + j], where
+ *    `ld` is the row stride (>= number of columns).
+ *  - Plain entry points take HOST pointers (a Rust Vec<T>'s buffer); the library copies
+ *    to the GPU, computes there and copies back. `_dev` entry points take DEVICE pointers
+ *    and a cudaStream_t passed as `void *` (NULL = the calling thread's default stream)
+ *    and are asynchronous unless stated otherwise.
+ *  - Permutations are the reference's stored form: a uint64_t per row, "row i -> perm[i]"
+ *    (PermutationMatrix{perm: Vec<usize>}, src/matrix/permutation_matrix.rs:102-111).
+ *  - Every function returns an rl_status. There is no CPU fallback: without a usable
+ *    GPU every compute entry point returns RL_ERR_NO_DEVICE.
+ *  - Thread safety: every call may come from any host thread; host-pointer calls run on
+ *    the per-thread default stream and block until their result is on the host.
+ */
+#ifndef RULINALG_GB300_H
+#define RULINALG_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define RL_API __attribute__((visibility("default")))
+#else
+#define RL_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. 1..6 map one to one onto rulinalg's ErrorKind (src/error.rs:21-34);
+ * RL_ERR_SHAPE is returned where the reference panics on a dimension assert!
+ * (e.g. src/matrix/mat_mul.rs:21, src/matrix/decomposition/lu.rs:165,232). */
+typedef int rl_status;
+#define RL_OK 0
+#define RL_ERR_INVALID_ARG 1
+#define RL_ERR_DECOMP_FAILURE 2
+#define RL_ERR_ALGEBRA_FAILURE 3
+#define RL_ERR_DIV_BY_ZERO 4
+#define RL_ERR_SCALAR_CONVERSION 5
+#define RL_ERR_INVALID_PERMUTATION 6
+#define RL_ERR_SHAPE 16
+#define RL_ERR_CUDA 32
+#define RL_ERR_NO_DEVICE 33
+#define RL_ERR_OUT_OF_MEMORY 34
+#define RL_ERR_TIMEOUT 35
+#define RL_ERR_NOT_CONVERGED 36
+
+/* Human-readable text for a status (static storage). */
+RL_API const char *rl_status_string(rl_status status);
+/* ABI version: major * 10000 + minor * 100 + patch. */
+RL_API int rl_version(void);
+/* RL_OK when a CUDA device of compute capability 10.3 is usable by this process. */
+RL_API rl_status rl_device_check(void);
+/* Number of kernel launches this library has issued in this process (all threads). */
+RL_API uint64_t rl_launch_count(void);
+
+/* ------------------------------------------------------------------------ GEMM -- */
+/* C = A * B with A m x k, B k x n, C m x n; alpha = 1, beta = 0.
+ * Replaces the matrixmultiply::{sgemm,dgemm} calls of mat_mul_general!
+ * (src/matrix/mat_mul.rs:33-43 and :57-67): rsa/rsb are the row strides that
+ * `row_stride()` supplies there, rsc = n for a new Matrix. */
+RL_API rl_status rl_sgemm(size_t m, size_t k, size_t n, const float *a, size_t rsa, const float *b, size_t rsb,
+                   float *c, size_t rsc);
+RL_API rl_status rl_dgemm(size_t m, size_t k, size_t n, const double *a, size_t rsa, const double *b, size_t rsb,
+                   double *c, size_t rsc);
+RL_API rl_status rl_sgemm_dev(size_t m, size_t k, size_t n, const float *a, size_t rsa, const float *b, size_t rsb,
+                       float *c, size_t rsc, void *stream);
+RL_API rl_status rl_dgemm_dev(size_t m, size_t k, size_t n, const double *a, size_t rsa, const double *b,
+                       size_t rsb, double *c, size_t rsc, void *stream);
+
+/* ---------------------------------------------------------------- PartialPivLu -- */
+/* PartialPivLu::decompose (src/matrix/decomposition/lu.rs:163-194): A (n x n, in place)
+ * becomes the compact LU (unit L strictly below the diagonal, U on and above it) and
+ * perm receives the stored permutation p with P A = L U. Pivoting takes the first
+ * largest |a[i,k]|; a pivot with |p| < epsilon returns RL_ERR_DIV_BY_ZERO. */
+RL_API rl_status rl_slu_decompose(size_t n, float *a, size_t lda, uint64_t *perm);
+RL_API rl_status rl_dlu_decompose(size_t n, double *a, size_t lda, uint64_t *perm);
+/* PartialPivLu::solve (lu.rs:231-244) for nrhs right-hand sides at once: B is n x nrhs
+ * (row-major, row stride ldb; nrhs = 1, ldb = 1 is a Vector<T>) and is overwritten by X.
+ * RL_ERR_DIV_BY_ZERO when |u_ii| < epsilon (src/matrix/mod.rs:333-336). */
+RL_API rl_status rl_slu_solve(size_t n, size_t nrhs, const float *lu, size_t lda, const uint64_t *perm, float *b,
+                       size_t ldb);
+RL_API rl_status rl_dlu_solve(size_t n, size_t nrhs, const double *lu, size_t lda, const uint64_t *perm, double *b,
+                       size_t ldb);
+/* PartialPivLu::inverse (lu.rs:251-285). */
+RL_API rl_status rl_slu_inverse(size_t n, const float *lu, size_t lda, const uint64_t *perm, float *inv, size_t ldi);
+RL_API rl_status rl_dlu_inverse(size_t n, const double *lu, size_t lda, const uint64_t *perm, double *inv,
+                         size_t ldi);
+/* PartialPivLu::det (lu.rs:291-300): prod(diag U) * det(P). */
+RL_API rl_status rl_slu_det(size_t n, const float *lu, size_t lda, const uint64_t *perm, float *det);
+RL_API rl_status rl_dlu_det(size_t n, const double *lu, size_t lda, const uint64_t *perm, double *det);
+
+/* -------------------------------------------------------------------- Cholesky -- */
+/* Cholesky::decompose (src/matrix/decomposition/cholesky.rs:116-169): the lower triangle
+ * of A (in place) becomes L with A = L L^T; the strict upper triangle is neither read nor
+ * written. |d| < epsilon or d < 0 on the diagonal returns RL_ERR_DECOMP_FAILURE. */
+RL_API rl_status rl_scholesky_decompose(size_t n, float *a, size_t lda);
+RL_API rl_status rl_dcholesky_decompose(size_t n, double *a, size_t lda);
+/* Cholesky::solve (cholesky.rs:194-202) for n x nrhs B, overwritten by X. */
+RL_API rl_status rl_scholesky_solve(size_t n, size_t nrhs, const float *l, size_t ldl, float *b, size_t ldb);
+RL_API rl_status rl_dcholesky_solve(size_t n, size_t nrhs, const double *l, size_t ldl, double *b, size_t ldb);
+/* Cholesky::inverse (cholesky.rs:209-234) and Cholesky::det (cholesky.rs:175-180). */
+RL_API rl_status rl_scholesky_inverse(size_t n, const float *l, size_t ldl, float *inv, size_t ldi);
+RL_API rl_status rl_dcholesky_inverse(size_t n, const double *l, size_t ldl, double *inv, size_t ldi);
+RL_API rl_status rl_scholesky_det(size_t n, const float *l, size_t ldl, float *det);
+RL_API rl_status rl_dcholesky_det(size_t n, const double *l, size_t ldl, double *det);
+
+/* --------------------------------------------------------------- HouseholderQr -- */
+/* HouseholderQr::decompose (src/matrix/decomposition/qr.rs:180-223): A (m x n, in place)
+ * becomes R on and above the diagonal and the Householder vectors v_j (implicit leading
+ * 1) below it; tau receives min(m, n) scale factors. Infallible in the reference. */
+RL_API rl_status rl_sqr_decompose(size_t m, size_t n, float *a, size_t lda, float *tau);
+RL_API rl_status rl_dqr_decompose(size_t m, size_t n, double *a, size_t lda, double *tau);
+/* HouseholderComposition::first_k_columns (householder.rs:235-268): the first k columns
+ * of Q (m x k) from the compact storage; k = m is QR::unpack's Q (qr.rs:278-296), k = n
+ * is unpack_thin's Q1 (qr.rs:250-275). */
+RL_API rl_status rl_sqr_first_k_columns(size_t m, size_t n, const float *qr, size_t lda, const float *tau, size_t k,
+                                 float *q, size_t ldq);
+RL_API rl_status rl_dqr_first_k_columns(size_t m, size_t n, const double *qr, size_t lda, const double *tau,
+                                 size_t k, double *q, size_t ldq);
+/* Least squares min ||A x - b||_2 for m >= n (no routine in the reference; it is the
+ * composition unpack_thin -> q1^T b -> r1.solve_u_triangular, qr.rs:250-275,
+ * src/matrix/base/mod.rs:1015-1024). A is consumed, b has m entries, x receives n.
+ * RL_ERR_DIV_BY_ZERO when |r_ii| < epsilon. */
+RL_API rl_status rl_sqr_least_squares(size_t m, size_t n, float *a, size_t lda, const float *b, float *x);
+RL_API rl_status rl_dqr_least_squares(size_t m, size_t n, double *a, size_t lda, const double *b, double *x);
+
+/* ---------------------------------------------------- Matrix::solve/inverse/det -- */
+/* Matrix::solve (src/matrix/impl_mat.rs:354-356): decompose + solve; A is consumed. */
+RL_API rl_status rl_smatrix_solve(size_t n, float *a, size_t lda, float *b);
+RL_API rl_status rl_dmatrix_solve(size_t n, double *a, size_t lda, double *b);
+/* Matrix::inverse (impl_mat.rs:386-388). A is consumed. */
+RL_API rl_status rl_smatrix_inverse(size_t n, float *a, size_t lda, float *inv, size_t ldi);
+RL_API rl_status rl_dmatrix_inverse(size_t n, double *a, size_t lda, double *inv, size_t ldi);
+/* Matrix::det (impl_mat.rs:407-427): closed forms for diagonal, 2x2 and 3x3, else
+ * PartialPivLu with a decomposition failure mapped to 0. A is consumed. */
+RL_API rl_status rl_smatrix_det(size_t n, float *a, size_t lda, float *det);
+RL_API rl_status rl_dmatrix_det(size_t n, double *a, size_t lda, double *det);
+
+/* ------------------------------------------------------------- batched solves -- */
+/* Thousands of independent systems A_i x_i = b_i (n_i <= 512, any mix of sizes and of
+ * PartialPivLu / Cholesky) solved in one launch. The reference has no batched routine:
+ * this replaces a caller's loop of `PartialPivLu::decompose(a)?.solve(b)`
+ * (lu.rs:163-244) or `Cholesky::decompose(a)?.solve(b)` (cholesky.rs:116-202).
+ *
+ * Packed layout: system i's matrix occupies n_i * n_i elements (row-major, row stride
+ * n_i) starting at a[a_offset[i]]; its right-hand side and solution occupy n_i elements
+ * at b[b_offset[i]] and x[b_offset[i]] (rl_batch_plan_layout gives the offsets).
+ *
+ * Precision of a plan:
+ *   RL_PREC_FP64  f64 systems, factor and solve in FP64 (the plain GPU path).
+ *   RL_PREC_MIXED f64 systems, factor in FP32, FP64 iterative refinement (residual,
+ *                 update and backward-error stopping test in FP64) to f64 accuracy;
+ *                 systems whose FP32 factor fails or whose refinement stalls are
+ *                 refactored in FP64 in the same launch sequence (iters = -1).
+ *   RL_PREC_FP32  f32 systems (Matrix<f32>), factor and solve in FP32.
+ * Per system: info (rl_status: DivByZero / DecompFailure as the reference would
+ * return), iters (refinement steps) and berr = ||b - A x||_inf /
+ * (||A||_inf ||x||_inf + ||b||_inf) computed in FP64. iters/berr may be NULL. */
+#define RL_KIND_LU 0
+#define RL_KIND_CHOLESKY 1
+#define RL_PREC_FP64 0
+#define RL_PREC_MIXED 1
+#define RL_PREC_FP32 2
+typedef struct rl_batch_plan rl_batch_plan;
+RL_API rl_status rl_batch_plan_create(rl_batch_plan **plan, size_t count, const int32_t *n, const uint8_t *kind,
+                               int precision);
+RL_API rl_status rl_batch_plan_destroy(rl_batch_plan *plan);
+RL_API rl_status rl_batch_plan_layout(const rl_batch_plan *plan, int64_t *a_offset, int64_t *b_offset, int64_t *a_total,
+                               int64_t *b_total);
+/* Device pointers; asynchronous on `stream`; the launch sequence is captured once as a
+ * CUDA graph per set of pointers and replayed. */
+RL_API rl_status rl_dbatch_solve_dev(rl_batch_plan *plan, const double *a, const double *b, double *x, int32_t *info,
+                              int32_t *iters, double *berr, void *stream);
+RL_API rl_status rl_sbatch_solve_dev(rl_batch_plan *plan, const float *a, const float *b, float *x, int32_t *info,
+                              int32_t *iters, double *berr, void *stream);
+/* Host pointers: copy in, solve, copy out; blocking. */
+RL_API rl_status rl_dbatch_solve(rl_batch_plan *plan, const double *a, const double *b, double *x, int32_t *info,
+                          int32_t *iters, double *berr);
+RL_API rl_status rl_sbatch_solve(rl_batch_plan *plan, const float *a, const float *b, float *x, int32_t *info,
+                          int32_t *iters, double *berr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RULINALG_GB300_H */

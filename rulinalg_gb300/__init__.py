@@ -1,0 +1,17 @@
+"""rulinalg_gb300: rulinalg's dense hot path (GEMM, PartialPivLu, Cholesky,
+HouseholderQr with solve/det/inverse) as hand-written sm_103a CUDA behind a C ABI
+(include/rulinalg_gb300.h). Importing loads librulinalg_gb300.so; there is no CPU path."""
+from ._lib import lib, LIB_PATH  # noqa: F401  (raises ImportError when the library is not built)
+from .api import (  # noqa: F401
+    Cholesky, DeviceError, HouseholderQr, LUP, PartialPivLu, PermutationMatrix, QR, RulinalgError,
+    RulinalgPanic, ThinQR, det, inverse, least_squares, mat_mul, solve,
+)
+from .batch import BatchPlan, KIND_CHOLESKY, KIND_LU, PREC_FP32, PREC_FP64, PREC_MIXED  # noqa: F401
+
+
+def device_available() -> bool:
+    return lib.rl_device_check() == 0
+
+
+def launch_count() -> int:
+    return int(lib.rl_launch_count())

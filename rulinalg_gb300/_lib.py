@@ -1,0 +1,84 @@
+"""ctypes binding of librulinalg_gb300.so (the C ABI declared in include/rulinalg_gb300.h).
+
+The library is the product: there is no Python or CPU implementation behind these
+names. If the shared object has not been built, importing raises immediately.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = Path(os.environ.get("RULINALG_GB300_LIB", _PKG / "librulinalg_gb300.so"))
+
+if not LIB_PATH.exists():
+    raise ImportError(
+        f"{LIB_PATH} is missing: build the CUDA library first "
+        "(python -c 'import __graft_entry__ as g; g.build()' or python rulinalg_gb300/build.py)")
+
+lib = C.CDLL(str(LIB_PATH))
+
+sz = C.c_size_t
+i64 = C.c_int64
+f32p = C.POINTER(C.c_float)
+f64p = C.POINTER(C.c_double)
+u64p = C.POINTER(C.c_uint64)
+i32p = C.POINTER(C.c_int32)
+u8p = C.POINTER(C.c_uint8)
+i64p = C.POINTER(C.c_int64)
+vp = C.c_void_p
+st = C.c_int
+
+# name -> (restype, argtypes). Every function the header declares appears here, and
+# tests check the two lists against each other.
+SIGNATURES = {
+    "rl_status_string": (C.c_char_p, [st]),
+    "rl_version": (C.c_int, []),
+    "rl_device_check": (st, []),
+    "rl_launch_count": (C.c_uint64, []),
+    "rl_sgemm": (st, [sz, sz, sz, f32p, sz, f32p, sz, f32p, sz]),
+    "rl_dgemm": (st, [sz, sz, sz, f64p, sz, f64p, sz, f64p, sz]),
+    "rl_sgemm_dev": (st, [sz, sz, sz, vp, sz, vp, sz, vp, sz, vp]),
+    "rl_dgemm_dev": (st, [sz, sz, sz, vp, sz, vp, sz, vp, sz, vp]),
+    "rl_slu_decompose": (st, [sz, f32p, sz, u64p]),
+    "rl_dlu_decompose": (st, [sz, f64p, sz, u64p]),
+    "rl_slu_solve": (st, [sz, sz, f32p, sz, u64p, f32p, sz]),
+    "rl_dlu_solve": (st, [sz, sz, f64p, sz, u64p, f64p, sz]),
+    "rl_slu_inverse": (st, [sz, f32p, sz, u64p, f32p, sz]),
+    "rl_dlu_inverse": (st, [sz, f64p, sz, u64p, f64p, sz]),
+    "rl_slu_det": (st, [sz, f32p, sz, u64p, f32p]),
+    "rl_dlu_det": (st, [sz, f64p, sz, u64p, f64p]),
+    "rl_scholesky_decompose": (st, [sz, f32p, sz]),
+    "rl_dcholesky_decompose": (st, [sz, f64p, sz]),
+    "rl_scholesky_solve": (st, [sz, sz, f32p, sz, f32p, sz]),
+    "rl_dcholesky_solve": (st, [sz, sz, f64p, sz, f64p, sz]),
+    "rl_scholesky_inverse": (st, [sz, f32p, sz, f32p, sz]),
+    "rl_dcholesky_inverse": (st, [sz, f64p, sz, f64p, sz]),
+    "rl_scholesky_det": (st, [sz, f32p, sz, f32p]),
+    "rl_dcholesky_det": (st, [sz, f64p, sz, f64p]),
+    "rl_sqr_decompose": (st, [sz, sz, f32p, sz, f32p]),
+    "rl_dqr_decompose": (st, [sz, sz, f64p, sz, f64p]),
+    "rl_sqr_first_k_columns": (st, [sz, sz, f32p, sz, f32p, sz, f32p, sz]),
+    "rl_dqr_first_k_columns": (st, [sz, sz, f64p, sz, f64p, sz, f64p, sz]),
+    "rl_sqr_least_squares": (st, [sz, sz, f32p, sz, f32p, f32p]),
+    "rl_dqr_least_squares": (st, [sz, sz, f64p, sz, f64p, f64p]),
+    "rl_smatrix_solve": (st, [sz, f32p, sz, f32p]),
+    "rl_dmatrix_solve": (st, [sz, f64p, sz, f64p]),
+    "rl_smatrix_inverse": (st, [sz, f32p, sz, f32p, sz]),
+    "rl_dmatrix_inverse": (st, [sz, f64p, sz, f64p, sz]),
+    "rl_smatrix_det": (st, [sz, f32p, sz, f32p]),
+    "rl_dmatrix_det": (st, [sz, f64p, sz, f64p]),
+    "rl_batch_plan_create": (st, [C.POINTER(vp), sz, i32p, u8p, C.c_int]),
+    "rl_batch_plan_destroy": (st, [vp]),
+    "rl_batch_plan_layout": (st, [vp, i64p, i64p, i64p, i64p]),
+    "rl_dbatch_solve_dev": (st, [vp, vp, vp, vp, vp, vp, vp, vp]),
+    "rl_sbatch_solve_dev": (st, [vp, vp, vp, vp, vp, vp, vp, vp]),
+    "rl_dbatch_solve": (st, [vp, f64p, f64p, f64p, i32p, i32p, f64p]),
+    "rl_sbatch_solve": (st, [vp, f32p, f32p, f32p, i32p, i32p, f64p]),
+}
+
+for _name, (_res, _args) in SIGNATURES.items():
+    _fn = getattr(lib, _name)
+    _fn.restype = _res
+    _fn.argtypes = _args

@@ -1,0 +1,313 @@
+// Batched solves: the plan object (sizes, packed layout, largest-first schedule,
+// per-CTA workspace slots, captured CUDA graph) and its C entry points.
+#include <algorithm>
+#include <mutex>
+#include <numeric>
+#include <type_traits>
+#include <vector>
+
+#include "batch.cuh"
+
+using namespace rl;
+
+struct rl_batch_plan {
+    int precision = RL_PREC_MIXED;
+    size_t count = 0;
+    int max_n = 0;
+    std::vector<int> n;
+    std::vector<uint8_t> kind;
+    std::vector<long long> a_off, b_off;
+    long long a_total = 0, b_total = 0;
+
+    int *d_n = nullptr, *d_order = nullptr, *d_counters = nullptr, *d_fb_list = nullptr;
+    uint8_t *d_kind = nullptr;
+    long long *d_aoff = nullptr, *d_boff = nullptr;
+    void *d_work = nullptr;   // factor-type slots of the main pass
+    double *d_work64 = nullptr;  // FP64 slots of the fallback pass (mixed)
+    long long work_stride = 0;
+    int grid = 0, grid64 = 0;
+    size_t smem = 0, smem64 = 0;
+
+    cudaStream_t cap = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    const void *key[6] = {};
+
+    // device copies used by the host-pointer entry points
+    void *h_a = nullptr, *h_b = nullptr, *h_x = nullptr;
+    int *h_info = nullptr, *h_iters = nullptr;
+    double *h_berr = nullptr;
+
+    std::mutex mu;
+};
+
+namespace {
+
+template <class TI, class TF, bool MIXED>
+rl_status occupancy_grid(size_t smem, int &grid) {
+    auto kern = batch_solve_kernel<TI, TF, MIXED>;
+    RL_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    RL_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, CTA_THREADS, smem));
+    if (per_sm < 1) return RL_ERR_CUDA;
+    grid = per_sm * num_sms();
+    return RL_OK;
+}
+
+template <class TI, class TF, bool MIXED>
+rl_status record(rl_batch_plan *p, const TI *a, const TI *b, TI *x, int *info, int *iters, double *berr,
+                 cudaStream_t s) {
+    RL_TRY_CUDA(cudaMemsetAsync(p->d_counters, 0, 4 * sizeof(int), s));
+    BatchDesc d{};
+    d.count = (int)p->count;
+    d.count_dev = nullptr;
+    d.order = p->d_order;
+    d.n = p->d_n;
+    d.kind = p->d_kind;
+    d.a_off = p->d_aoff;
+    d.b_off = p->d_boff;
+    d.next = p->d_counters;
+    d.fb_list = p->d_fb_list;
+    d.fb_count = p->d_counters + 1;
+    d.work = p->d_work;
+    d.work_stride = p->work_stride;
+    d.info = info;
+    d.iters = iters;
+    d.berr = berr;
+    d.iters_tag = 0;
+    d.max_iters = 30;
+    RL_LAUNCH((batch_solve_kernel<TI, TF, MIXED>), p->grid, CTA_THREADS, p->smem, s, d, a, b, x);
+    if (MIXED) {
+        BatchDesc f = d;
+        f.count = 0;
+        f.count_dev = p->d_counters + 1;
+        f.order = p->d_fb_list;
+        f.next = p->d_counters + 2;
+        f.work = p->d_work64;
+        f.iters_tag = -1;
+        RL_LAUNCH((batch_solve_kernel<TI, double, false>), p->grid64, CTA_THREADS, p->smem64, s, f, a, b, x);
+    }
+    return RL_OK;
+}
+
+template <class TI, class TF, bool MIXED>
+rl_status run_plan(rl_batch_plan *p, const TI *a, const TI *b, TI *x, int *info, int *iters, double *berr,
+                   cudaStream_t s) {
+    const void *key[6] = {a, b, x, info, iters, berr};
+    if (!p->exec || !std::equal(key, key + 6, p->key)) {
+        if (p->exec) {
+            cudaGraphExecDestroy(p->exec);
+            p->exec = nullptr;
+        }
+        RL_TRY_CUDA(cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal));
+        const uint64_t before = g_launches.load();
+        rl_status st = record<TI, TF, MIXED>(p, a, b, x, info, iters, berr, p->cap);
+        g_launches.store(before);  // capture does not launch anything
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(p->cap, &g);
+        if (st != RL_OK) {
+            if (g) cudaGraphDestroy(g);
+            return st;
+        }
+        if (e != cudaSuccess) return from_cuda(e);
+        e = cudaGraphInstantiate(&p->exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            p->exec = nullptr;
+            return from_cuda(e);
+        }
+        std::copy(key, key + 6, p->key);
+    }
+    RL_TRY_CUDA(cudaGraphLaunch(p->exec, s));
+    count_launch(MIXED ? 2 : 1);
+    return RL_OK;
+}
+
+template <class TI>
+rl_status solve_host(rl_batch_plan *p, const TI *a, const TI *b, TI *x, int32_t *info, int32_t *iters,
+                     double *berr) {
+    cudaStream_t s = cudaStreamPerThread;
+    if (!p->h_a) {
+        RL_TRY_CUDA(cudaMalloc(&p->h_a, std::max<long long>(1, p->a_total) * sizeof(TI)));
+        RL_TRY_CUDA(cudaMalloc(&p->h_b, std::max<long long>(1, p->b_total) * sizeof(TI)));
+        RL_TRY_CUDA(cudaMalloc(&p->h_x, std::max<long long>(1, p->b_total) * sizeof(TI)));
+        RL_TRY_CUDA(cudaMalloc(&p->h_info, std::max<size_t>(1, p->count) * sizeof(int)));
+        RL_TRY_CUDA(cudaMalloc(&p->h_iters, std::max<size_t>(1, p->count) * sizeof(int)));
+        RL_TRY_CUDA(cudaMalloc(&p->h_berr, std::max<size_t>(1, p->count) * sizeof(double)));
+    }
+    TI *da = static_cast<TI *>(p->h_a), *db = static_cast<TI *>(p->h_b), *dx = static_cast<TI *>(p->h_x);
+    if (p->a_total) RL_TRY_CUDA(cudaMemcpyAsync(da, a, p->a_total * sizeof(TI), cudaMemcpyHostToDevice, s));
+    if (p->b_total) RL_TRY_CUDA(cudaMemcpyAsync(db, b, p->b_total * sizeof(TI), cudaMemcpyHostToDevice, s));
+    rl_status st;
+    if (std::is_same<TI, float>::value)
+        st = run_plan<float, float, false>(p, (const float *)da, (const float *)db, (float *)dx, p->h_info,
+                                           p->h_iters, p->h_berr, s);
+    else if (p->precision == RL_PREC_MIXED)
+        st = run_plan<double, float, true>(p, (const double *)da, (const double *)db, (double *)dx, p->h_info,
+                                           p->h_iters, p->h_berr, s);
+    else
+        st = run_plan<double, double, false>(p, (const double *)da, (const double *)db, (double *)dx, p->h_info,
+                                             p->h_iters, p->h_berr, s);
+    RL_TRY(st);
+    if (p->b_total) RL_TRY_CUDA(cudaMemcpyAsync(x, dx, p->b_total * sizeof(TI), cudaMemcpyDeviceToHost, s));
+    if (info && p->count) RL_TRY_CUDA(cudaMemcpyAsync(info, p->h_info, p->count * sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (iters && p->count)
+        RL_TRY_CUDA(cudaMemcpyAsync(iters, p->h_iters, p->count * sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (berr && p->count)
+        RL_TRY_CUDA(cudaMemcpyAsync(berr, p->h_berr, p->count * sizeof(double), cudaMemcpyDeviceToHost, s));
+    RL_TRY_CUDA(cudaStreamSynchronize(s));
+    return RL_OK;
+}
+
+template <class T>
+rl_status upload(T *&dst, const std::vector<T> &src, cudaStream_t s) {
+    RL_TRY_CUDA(cudaMalloc(&dst, std::max<size_t>(1, src.size()) * sizeof(T)));
+    if (!src.empty()) RL_TRY_CUDA(cudaMemcpyAsync(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    return RL_OK;
+}
+
+rl_status plan_init(rl_batch_plan *p, size_t count, const int32_t *n, const uint8_t *kind, int precision) {
+    p->precision = precision;
+    p->count = count;
+    p->n.resize(count);
+    p->kind.resize(count);
+    p->a_off.resize(count);
+    p->b_off.resize(count);
+    long long a = 0, b = 0;
+    for (size_t i = 0; i < count; i++) {
+        if (n[i] < 0 || n[i] > CTA_NMAX) return RL_ERR_INVALID_ARG;
+        if (kind && kind[i] > 1) return RL_ERR_INVALID_ARG;
+        p->n[i] = n[i];
+        p->kind[i] = kind ? kind[i] : 0;
+        p->a_off[i] = a;
+        p->b_off[i] = b;
+        a += (long long)n[i] * n[i];
+        b += n[i];
+        p->max_n = std::max(p->max_n, (int)n[i]);
+    }
+    p->a_total = a;
+    p->b_total = b;
+    // Largest work first (LU costs twice Cholesky), so the tail of the launch is short.
+    std::vector<int> order(count);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        const double cx = (double)p->n[x] * p->n[x] * p->n[x] * (p->kind[x] ? 1.0 : 2.0);
+        const double cy = (double)p->n[y] * p->n[y] * p->n[y] * (p->kind[y] ? 1.0 : 2.0);
+        return cx > cy;
+    });
+    cudaStream_t s = cudaStreamPerThread;
+    RL_TRY(upload(p->d_n, p->n, s));
+    RL_TRY(upload(p->d_kind, p->kind, s));
+    RL_TRY(upload(p->d_aoff, p->a_off, s));
+    RL_TRY(upload(p->d_boff, p->b_off, s));
+    RL_TRY(upload(p->d_order, order, s));
+    RL_TRY_CUDA(cudaMalloc(&p->d_counters, 4 * sizeof(int)));
+    RL_TRY_CUDA(cudaMalloc(&p->d_fb_list, std::max<size_t>(1, count) * sizeof(int)));
+    p->work_stride = std::max(1LL, (long long)p->max_n * p->max_n);
+    if (precision == RL_PREC_MIXED) {
+        p->smem = cta_smem_bytes<float>();
+        RL_TRY((occupancy_grid<double, float, true>(p->smem, p->grid)));
+        p->smem64 = cta_smem_bytes<double>();
+        RL_TRY((occupancy_grid<double, double, false>(p->smem64, p->grid64)));
+        RL_TRY_CUDA(cudaMalloc(&p->d_work, p->grid * p->work_stride * sizeof(float)));
+        RL_TRY_CUDA(cudaMalloc(&p->d_work64, p->grid64 * p->work_stride * sizeof(double)));
+    } else if (precision == RL_PREC_FP64) {
+        p->smem = cta_smem_bytes<double>();
+        RL_TRY((occupancy_grid<double, double, false>(p->smem, p->grid)));
+        RL_TRY_CUDA(cudaMalloc(&p->d_work, p->grid * p->work_stride * sizeof(double)));
+    } else if (precision == RL_PREC_FP32) {
+        p->smem = cta_smem_bytes<float>();
+        RL_TRY((occupancy_grid<float, float, false>(p->smem, p->grid)));
+        RL_TRY_CUDA(cudaMalloc(&p->d_work, p->grid * p->work_stride * sizeof(float)));
+    } else {
+        return RL_ERR_INVALID_ARG;
+    }
+    RL_TRY_CUDA(cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking));
+    RL_TRY_CUDA(cudaStreamSynchronize(s));
+    return RL_OK;
+}
+
+void plan_free(rl_batch_plan *p) {
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->cap) cudaStreamDestroy(p->cap);
+    void *ptrs[] = {p->d_n, p->d_order, p->d_counters, p->d_fb_list, p->d_kind, p->d_aoff, p->d_boff, p->d_work,
+                    p->d_work64, p->h_a, p->h_b, p->h_x, p->h_info, p->h_iters, p->h_berr};
+    for (void *q : ptrs)
+        if (q) cudaFree(q);
+}
+
+}  // namespace
+
+extern "C" {
+
+rl_status rl_batch_plan_create(rl_batch_plan **plan, size_t count, const int32_t *n, const uint8_t *kind,
+                               int precision) {
+    if (!plan || (count && !n)) return RL_ERR_INVALID_ARG;
+    *plan = nullptr;
+    if (count > (size_t)INT32_MAX) return RL_ERR_INVALID_ARG;
+    RL_TRY(ensure_device());
+    rl_batch_plan *p = new rl_batch_plan();
+    rl_status st = plan_init(p, count, n, kind, precision);
+    if (st != RL_OK) {
+        plan_free(p);
+        delete p;
+        return st;
+    }
+    *plan = p;
+    return RL_OK;
+}
+
+rl_status rl_batch_plan_destroy(rl_batch_plan *plan) {
+    if (!plan) return RL_OK;
+    cudaDeviceSynchronize();
+    plan_free(plan);
+    delete plan;
+    return RL_OK;
+}
+
+rl_status rl_batch_plan_layout(const rl_batch_plan *plan, int64_t *a_offset, int64_t *b_offset, int64_t *a_total,
+                               int64_t *b_total) {
+    if (!plan) return RL_ERR_INVALID_ARG;
+    for (size_t i = 0; i < plan->count; i++) {
+        if (a_offset) a_offset[i] = plan->a_off[i];
+        if (b_offset) b_offset[i] = plan->b_off[i];
+    }
+    if (a_total) *a_total = plan->a_total;
+    if (b_total) *b_total = plan->b_total;
+    return RL_OK;
+}
+
+rl_status rl_dbatch_solve_dev(rl_batch_plan *plan, const double *a, const double *b, double *x, int32_t *info,
+                              int32_t *iters, double *berr, void *stream) {
+    if (!plan || !info || (plan->b_total && (!a || !b || !x))) return RL_ERR_INVALID_ARG;
+    if (plan->precision == RL_PREC_FP32) return RL_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(plan->mu);
+    cudaStream_t s = resolve_stream(stream);
+    if (plan->precision == RL_PREC_MIXED) return run_plan<double, float, true>(plan, a, b, x, info, iters, berr, s);
+    return run_plan<double, double, false>(plan, a, b, x, info, iters, berr, s);
+}
+
+rl_status rl_sbatch_solve_dev(rl_batch_plan *plan, const float *a, const float *b, float *x, int32_t *info,
+                              int32_t *iters, double *berr, void *stream) {
+    if (!plan || !info || (plan->b_total && (!a || !b || !x))) return RL_ERR_INVALID_ARG;
+    if (plan->precision != RL_PREC_FP32) return RL_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(plan->mu);
+    return run_plan<float, float, false>(plan, a, b, x, info, iters, berr, resolve_stream(stream));
+}
+
+rl_status rl_dbatch_solve(rl_batch_plan *plan, const double *a, const double *b, double *x, int32_t *info,
+                          int32_t *iters, double *berr) {
+    if (!plan || (plan->b_total && (!a || !b || !x))) return RL_ERR_INVALID_ARG;
+    if (plan->precision == RL_PREC_FP32) return RL_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(plan->mu);
+    return solve_host<double>(plan, a, b, x, info, iters, berr);
+}
+
+rl_status rl_sbatch_solve(rl_batch_plan *plan, const float *a, const float *b, float *x, int32_t *info,
+                          int32_t *iters, double *berr) {
+    if (!plan || (plan->b_total && (!a || !b || !x))) return RL_ERR_INVALID_ARG;
+    if (plan->precision != RL_PREC_FP32) return RL_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(plan->mu);
+    return solve_host<float>(plan, a, b, x, info, iters, berr);
+}
+
+}  // extern "C"

@@ -1,0 +1,458 @@
+// Kernels of the blocked (multi-CTA) factorisations used for n > 512 and for every
+// HouseholderQr: cooperative panel kernels with a bounded grid barrier, row swaps,
+// diagonal-block triangular solves and the compact-WY T factor. Trailing updates are
+// GEMMs (gemm.cuh).
+#pragma once
+
+#include <climits>
+
+#include "factor_cta.cuh"
+
+namespace rl {
+
+// Largest panel width of the blocked paths.
+template <class T>
+struct PanelNB {
+    static constexpr int value = 64;
+};
+
+// ------------------------------------------------------------------ grid barrier --
+// All CTAs of a cooperative launch arrive on `ctr`; thread 0 spins (bounded by
+// kBarrierTimeoutNs of wall time) until the count reaches `target`. On timeout the
+// error word is set and every CTA leaves the kernel at its next barrier.
+constexpr unsigned long long kBarrierTimeoutNs = 1000000000ull;  // 1 s
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ bool grid_barrier(unsigned *ctr, unsigned target, int *err) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(ctr, 1u);
+        const unsigned long long t0 = global_ns();
+        int ok = 1;
+        for (;;) {
+            if (ld_acquire_u32(ctr) >= target) break;
+            if (*(volatile int *)err != 0) {
+                ok = 0;
+                break;
+            }
+            if (global_ns() - t0 > kBarrierTimeoutNs) {
+                atomicCAS(err, 0, RL_ERR_TIMEOUT);
+                ok = 0;
+                break;
+            }
+            __nanosleep(64);
+        }
+        __threadfence();
+        s_ok = ok && (*(volatile int *)err == 0);
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// Shared state of one cooperative panel launch (global memory, zeroed per launch).
+struct PanelSync {
+    unsigned ctr;
+    int err;     // RL_ERR_TIMEOUT or a numerical status, first writer wins
+    int pad[2];
+};
+
+// ------------------------------------------------------------------- LU panel --
+// Factors the panel rows [0, mrows) x cols [0, kb) of `P` (row stride lda; P points at
+// A[k0][k0]) with partial pivoting. CTA g owns rows [g*rows_per, ...) staged in shared
+// memory row-major (stride NB + 1). Per column: local argmax -> publish candidate row
+// -> one grid barrier -> every CTA picks the same winner (largest |v|, smallest row on
+// ties), swaps, scales and updates its rows. ipiv receives k0-based global pivots.
+// cand: 2 slots x G x (2 + NB) values, rowj: 2 slots x NB values.
+template <class T>
+__global__ void __launch_bounds__(256) lu_panel_kernel(T *P, long long lda, int mrows, int kb, int k0, int rows_per,
+                                                       int *ipiv, T *cand, T *rowj, PanelSync *sync, T tiny) {
+    constexpr int NB = PanelNB<T>::value;
+    constexpr int LDR = NB + 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *R = reinterpret_cast<T *>(smem_raw);  // rows_per x LDR
+    T *prow = R + (size_t)rows_per * LDR;    // pivot row copy (NB)
+    __shared__ T s_v[8];
+    __shared__ int s_i[8];
+    const int G = gridDim.x, g = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int r0 = g * rows_per, r1 = min(mrows, r0 + rows_per), nr = max(0, r1 - r0);
+    const int CS = 2 + NB;  // candidate record: |v|, row, then the row's values
+
+    for (int idx = tid; idx < nr * kb; idx += blockDim.x) {
+        const int r = idx / kb, c = idx - r * kb;
+        R[r * LDR + c] = P[(long long)(r0 + r) * lda + c];
+    }
+    __syncthreads();
+    for (int j = 0; j < kb; j++) {
+        const int slot = j & 1;
+        T bv = T(-1);
+        int bi = INT_MAX;
+        for (int r = max(j - r0, 0) + tid; r < nr; r += blockDim.x) {
+            const T v = absT(R[r * LDR + j]);
+            if (v > bv) {
+                bv = v;
+                bi = r0 + r;
+            }
+        }
+        warp_amax(bv, bi);
+        if (lane == 0) {
+            s_v[warp] = bv;
+            s_i[warp] = bi;
+        }
+        __syncthreads();
+        bv = s_v[0];
+        bi = s_i[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) amax_combine(bv, bi, s_v[w], s_i[w]);
+        T *mine = cand + ((size_t)slot * G + g) * CS;
+        if (tid == 0) {
+            mine[0] = bv;
+            mine[1] = (T)(bi == INT_MAX ? -1 : bi);
+        }
+        if (bi != INT_MAX && tid < kb) mine[2 + tid] = R[(bi - r0) * LDR + tid];
+        if (j >= r0 && j < r1 && tid < kb) rowj[slot * NB + tid] = R[(j - r0) * LDR + tid];
+        if (!grid_barrier(&sync->ctr, (unsigned)(G * (j + 1)), &sync->err)) return;
+        // Winner over all CTAs, identical in every CTA.
+        T wv = T(-1);
+        int wi = INT_MAX, wg = -1;
+        for (int q = 0; q < G; q++) {
+            const volatile T *c = cand + ((size_t)slot * G + q) * CS;
+            const T v = c[0];
+            const int i = (int)c[1];
+            if (i < 0) continue;
+            if (v > wv || (v == wv && i < wi)) {
+                wv = v;
+                wi = i;
+                wg = q;
+            }
+        }
+        if (wi == INT_MAX) {  // no finite candidate (NaN column): keep the diagonal
+            wi = j;
+            wg = -1;
+        }
+        if (wg >= 0 && wv < tiny) {
+            if (g == 0 && tid == 0) atomicCAS(&sync->err, 0, RL_ERR_DIV_BY_ZERO);
+            return;
+        }
+        if (tid < kb) {
+            T v;
+            if (wg >= 0)
+                v = ((volatile T *)(cand + ((size_t)slot * G + wg) * CS))[2 + tid];
+            else
+                v = ((volatile T *)rowj)[slot * NB + tid];
+            prow[tid] = v;
+        }
+        __syncthreads();
+        if (wi != j) {
+            if (j >= r0 && j < r1 && tid < kb) R[(j - r0) * LDR + tid] = prow[tid];
+            if (wi >= r0 && wi < r1 && tid < kb) R[(wi - r0) * LDR + tid] = ((volatile T *)rowj)[slot * NB + tid];
+        }
+        if (g == 0 && tid == 0) ipiv[j] = k0 + wi;
+        __syncthreads();
+        const T p = prow[j];
+        for (int r = max(j + 1 - r0, 0) + tid; r < nr; r += blockDim.x) {
+            T *row = R + r * LDR;
+            const T l = row[j] / p;
+            row[j] = l;
+            for (int c = j + 1; c < kb; c++) row[c] = fma(-l, prow[c], row[c]);
+        }
+        __syncthreads();
+    }
+    for (int idx = tid; idx < nr * kb; idx += blockDim.x) {
+        const int r = idx / kb, c = idx - r * kb;
+        P[(long long)(r0 + r) * lda + c] = R[r * LDR + c];
+    }
+}
+
+// ------------------------------------------------------------ Householder panel --
+// Unblocked Householder QR of the panel rows [0, mrows) x cols [0, kb) (P points at
+// A[k0][k0]), reflector by reflector exactly as HouseholderReflection::compute and
+// buffered_left_multiply_into (householder.rs:32-130) but with the reductions split
+// over CTAs: sigma = dot(x[1..], x[1..]) and u = A^T v are summed from per-CTA partials
+// in CTA order after a grid barrier. Two barriers per column. tau receives kb values.
+// part: 2 slots x G x (1 + NB) partial sums; x0buf: 2 slots.
+template <class T>
+__global__ void __launch_bounds__(256) qr_panel_kernel(T *P, long long lda, int mrows, int kb, int rows_per, T *tau,
+                                                       T *part, T *x0buf, PanelSync *sync) {
+    constexpr int NB = PanelNB<T>::value;
+    constexpr int LDR = NB + 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *R = reinterpret_cast<T *>(smem_raw);  // rows_per x LDR
+    T *u = R + (size_t)rows_per * LDR;       // NB
+    __shared__ T s_red[8][NB + 1];
+    const int G = gridDim.x, g = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nw = blockDim.x >> 5;
+    const int r0 = g * rows_per, r1 = min(mrows, r0 + rows_per), nr = max(0, r1 - r0);
+    const int PS = 1 + NB;
+    for (int idx = tid; idx < nr * kb; idx += blockDim.x) {
+        const int r = idx / kb, c = idx - r * kb;
+        R[r * LDR + c] = P[(long long)(r0 + r) * lda + c];
+    }
+    __syncthreads();
+    unsigned phase = 0;
+    for (int j = 0; j < kb; j++) {
+        const int slot = j & 1;
+        // (1) sigma partial over rows > j, in row order per thread then tree order.
+        T s = T(0);
+        for (int r = max(j + 1 - r0, 0) + tid; r < nr; r += blockDim.x) {
+            const T v = R[r * LDR + j];
+            s = fma(v, v, s);
+        }
+        s = warp_sum(s);
+        if (lane == 0) s_red[warp][0] = s;
+        __syncthreads();
+        if (tid == 0) {
+            T t = T(0);
+            for (int w = 0; w < nw; w++) t += s_red[w][0];
+            part[((size_t)slot * G + g) * PS] = t;
+            if (j >= r0 && j < r1) x0buf[slot] = R[(j - r0) * LDR + j];
+        }
+        if (!grid_barrier(&sync->ctr, (unsigned)(G * (++phase)), &sync->err)) return;
+        T sigma = T(0);
+        for (int q = 0; q < G; q++) sigma += ((volatile T *)part)[((size_t)slot * G + q) * PS];
+        const T x0 = ((volatile T *)x0buf)[slot];
+        if (sigma == T(0)) {  // already a multiple of e1: tau = 0, nothing changes
+            if (g == 0 && tid == 0) tau[j] = T(0);
+            if (!grid_barrier(&sync->ctr, (unsigned)(G * (++phase)), &sync->err)) return;
+            continue;
+        }
+        const T x_norm = sqrt(x0 * x0 + sigma);
+        const T v0 = x0 > T(0) ? x0 + x_norm : x0 - x_norm;
+        const T two = T(2);
+        const T t = two * v0 * v0 / (v0 * v0 + sigma);
+        if (g == 0 && tid == 0) tau[j] = t;
+        // (2) u_c = sum_r v_r a[r][c] for c >= j over owned rows r >= j, with
+        // v_r = x_r / v0 (v_j = 1) formed on the fly so that column j still holds x.
+        for (int c = j + warp; c < kb; c += nw) {
+            T acc = T(0);
+            for (int r = max(j - r0, 0) + lane; r < nr; r += 32) {
+                const T vr = (r0 + r == j) ? T(1) : R[r * LDR + j] / v0;
+                acc = fma(vr, R[r * LDR + c], acc);
+            }
+            acc = warp_sum(acc);
+            if (lane == 0) part[((size_t)slot * G + g) * PS + 1 + c] = acc;
+        }
+        if (!grid_barrier(&sync->ctr, (unsigned)(G * (++phase)), &sync->err)) return;
+        if (tid >= j && tid < kb) {
+            T a = T(0);
+            for (int q = 0; q < G; q++) a += ((volatile T *)part)[((size_t)slot * G + q) * PS + 1 + tid];
+            u[tid] = a;
+        }
+        __syncthreads();
+        // (3) a[r][c] += (-tau v_r) u_c for c > j (ger, internal_utils.rs:67-83); the
+        // diagonal becomes x0 - tau u_j and v[1..] is stored below it (store_in_col).
+        for (int r = max(j - r0, 0) + tid; r < nr; r += blockDim.x) {
+            T *row = R + r * LDR;
+            const bool diag = (r0 + r == j);
+            const T vr = diag ? T(1) : row[j] / v0;
+            const T sc = -t * vr;
+            for (int c = j + 1; c < kb; c++) row[c] = fma(sc, u[c], row[c]);
+            row[j] = diag ? x0 - t * u[j] : vr;
+        }
+        __syncthreads();
+    }
+    for (int idx = tid; idx < nr * kb; idx += blockDim.x) {
+        const int r = idx / kb, c = idx - r * kb;
+        P[(long long)(r0 + r) * lda + c] = R[r * LDR + c];
+    }
+}
+
+// ------------------------------------------------------------------- row swaps --
+// Applies ipiv[j0..j1) (global rows; step j swaps rows j and ipiv[j]) to the columns
+// [0, c_skip0) and [c_skip1, ncols) of A. Thread per column, swaps in order.
+template <class T>
+__global__ void laswp_kernel(T *A, long long lda, int ncols, int c_skip0, int c_skip1, const int *ipiv, int j0,
+                             int j1) {
+    const int nother = ncols - (c_skip1 - c_skip0);
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nother) return;
+    const int gc = c < c_skip0 ? c : c + (c_skip1 - c_skip0);
+    for (int j = j0; j < j1; j++) {
+        const int p = ipiv[j];
+        if (p != j) {
+            T *a = A + (long long)j * lda + gc;
+            T *b = A + (long long)p * lda + gc;
+            const T t = *a;
+            *a = *b;
+            *b = t;
+        }
+    }
+}
+
+// ------------------------------------------------------- diagonal-block solves --
+// Solves op(D) X = Y in place for the bs x bs diagonal block D (bs <= 64, row stride
+// ldd) and Y = bs x nrhs (row stride ldy). mode 0: D unit lower; 1: D lower; 2: D upper;
+// 3: D^T with D lower (L^T). One thread per right-hand-side column. |d_ii| < tiny
+// (modes 1-3) records RL_ERR_DIV_BY_ZERO in status.
+template <class T>
+__global__ void __launch_bounds__(64) trsm_diag_kernel(const T *D, long long ldd, int bs, T *Y, long long ldy,
+                                                       int nrhs, int mode, int *status, T tiny) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T (*Ds)[65] = reinterpret_cast<T (*)[65]>(smem_raw);             // 64 x 65
+    T (*Ys)[64] = reinterpret_cast<T (*)[64]>(smem_raw + sizeof(T) * 64 * 65);  // 64 x 64
+    const int t = threadIdx.x;
+    const int c = blockIdx.x * 64 + t;
+    for (int idx = t; idx < bs * bs; idx += 64) {
+        const int i = idx / bs, j = idx - i * bs;
+        Ds[i][j] = D[(long long)i * ldd + j];
+    }
+    if (c < nrhs)
+        for (int i = 0; i < bs; i++) Ys[i][t] = Y[(long long)i * ldy + c];
+    __syncthreads();
+    if (c >= nrhs) return;
+    int bad = 0;
+    if (mode == 0 || mode == 1) {
+        for (int i = 0; i < bs; i++) {
+            T s = Ys[i][t];
+            for (int j = 0; j < i; j++) s = fma(-Ds[i][j], Ys[j][t], s);
+            if (mode == 1) {
+                if (absT(Ds[i][i]) < tiny) bad = 1;
+                s = s / Ds[i][i];
+            }
+            Ys[i][t] = s;
+        }
+    } else {
+        for (int i = bs - 1; i >= 0; i--) {
+            T s = Ys[i][t];
+            if (mode == 2)
+                for (int j = i + 1; j < bs; j++) s = fma(-Ds[i][j], Ys[j][t], s);
+            else
+                for (int j = i + 1; j < bs; j++) s = fma(-Ds[j][i], Ys[j][t], s);
+            if (absT(Ds[i][i]) < tiny) bad = 1;
+            Ys[i][t] = s / Ds[i][i];
+        }
+    }
+    if (bad) {
+        atomicCAS(status, 0, RL_ERR_DIV_BY_ZERO);
+        return;
+    }
+    for (int i = 0; i < bs; i++) Y[(long long)i * ldy + c] = Ys[i][t];
+}
+
+// Row-wise solve X D^T = Y for the rows of Y (m x bs, stride ldy), D lower bs x bs:
+// the Cholesky panel L21 = A21 L11^-T. Thread per row.
+template <class T>
+__global__ void __launch_bounds__(128) trsm_right_lt_kernel(const T *D, long long ldd, int bs, T *Y, long long ldy,
+                                                            int m) {
+    __shared__ T Ds[64][65];
+    for (int idx = threadIdx.x; idx < bs * bs; idx += blockDim.x) {
+        const int i = idx / bs, j = idx - i * bs;
+        Ds[i][j] = D[(long long)i * ldd + j];
+    }
+    __syncthreads();
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= m) return;
+    T *y = Y + (long long)r * ldy;
+    T x[64];
+#pragma unroll
+    for (int j = 0; j < 64; j++)
+        if (j < bs) x[j] = y[j];
+#pragma unroll
+    for (int j = 0; j < 64; j++) {
+        if (j < bs) {
+            T s = x[j];
+#pragma unroll
+            for (int i = 0; i < 64; i++)
+                if (i < j) s = fma(-x[i], Ds[j][i], s);
+            x[j] = s / Ds[j][j];
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 64; j++)
+        if (j < bs) y[j] = x[j];
+}
+
+// ------------------------------------------------------------- compact WY helpers --
+// V (mrows x kb, row stride kb) = the panel's reflectors with the implicit unit diagonal
+// and zeros above it.
+template <class T>
+__global__ void extract_v_kernel(const T *P, long long lda, int mrows, int kb, T *V) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)mrows * kb) return;
+    const int r = (int)(idx / kb), c = (int)(idx - (long long)r * kb);
+    V[idx] = r > c ? P[(long long)r * lda + c] : (r == c ? T(1) : T(0));
+}
+
+// T factor of H_0 ... H_{kb-1} = I - V T V^T (upper triangular, kb x kb) from the
+// Gram matrix Gm = V^T V and tau: T[j][j] = tau_j, T[0:j, j] = -tau_j T[0:j, 0:j] Gm[0:j, j].
+template <class T>
+__global__ void larft_kernel(const T *Gm, const T *tau, int kb, T *Tm) {
+    __shared__ T w[64];
+    const int t = threadIdx.x;
+    for (int idx = t; idx < kb * kb; idx += blockDim.x) Tm[idx] = T(0);
+    __syncthreads();
+    for (int j = 0; j < kb; j++) {
+        const T tj = tau[j];
+        if (t < j) {
+            T s = T(0);
+            for (int q = t; q < j; q++) s = fma(Tm[t * kb + q], Gm[q * kb + j], s);
+            w[t] = -tj * s;
+        }
+        __syncthreads();
+        if (t < j) Tm[t * kb + j] = w[t];
+        if (t == 0) Tm[j * kb + j] = tj;
+        __syncthreads();
+    }
+}
+
+// Identity-like start for first_k_columns: Q (m x k) = I[:, 0:k].
+template <class T>
+__global__ void eye_kernel(T *Q, long long ldq, int m, int k) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)m * k) return;
+    const int r = (int)(idx / k), c = (int)(idx - (long long)r * k);
+    Q[(long long)r * ldq + c] = r == c ? T(1) : T(0);
+}
+
+// Gathers rows: Y[perm[i]][:] = B[i][:] (the reference's P * b, applied to nrhs columns).
+template <class T>
+__global__ void permute_rows_kernel(const T *B, long long ldb, T *Y, long long ldy, int n, int nrhs,
+                                    const uint64_t *perm) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)n * nrhs) return;
+    const int i = (int)(idx / nrhs), c = (int)(idx - (long long)i * nrhs);
+    Y[(long long)perm[i] * ldy + c] = B[(long long)i * ldb + c];
+}
+
+// det helpers: sequential fold of the diagonal in row order (the reference's fold), and
+// the parity of a stored permutation by cycle resolution (permutation_matrix.rs:479-509).
+template <class T>
+__global__ void det_kernel(const T *A, long long lda, int n, const uint64_t *perm, uint64_t *scratch, int square,
+                           T *out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    T d = T(1);
+    for (int i = 0; i < n; i++) d = d * A[(long long)i * lda + i];
+    if (square) {
+        out[0] = d * d;
+        return;
+    }
+    int odd = 0;
+    if (perm) {
+        for (int i = 0; i < n; i++) scratch[i] = perm[i];
+        for (int i = 0; i < n; i++) {
+            uint64_t target = scratch[i];
+            while ((uint64_t)i != target) {
+                const uint64_t nt = scratch[target];
+                odd ^= 1;
+                scratch[target] = target;
+                target = nt;
+            }
+            scratch[i] = i;
+        }
+    }
+    const T p_det = odd ? T(0) - T(1) : T(1);
+    out[0] = p_det * d;
+}
+
+}  // namespace rl

@@ -1,0 +1,90 @@
+// Process-wide runtime state of the library: device check, memory-pool set-up, status
+// strings and the launch counter.
+#include <mutex>
+
+#include "common.cuh"
+
+namespace rl {
+
+std::atomic<uint64_t> g_launches{0};
+
+static std::once_flag g_dev_once;
+static rl_status g_dev_status = RL_ERR_NO_DEVICE;
+static int g_num_sms = 0;
+
+rl_status from_cuda(cudaError_t e) {
+    if (e == cudaSuccess) return RL_OK;
+    if (e == cudaErrorMemoryAllocation) return RL_ERR_OUT_OF_MEMORY;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return RL_ERR_NO_DEVICE;
+    return RL_ERR_CUDA;
+}
+
+static void init_device() {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        g_dev_status = RL_ERR_NO_DEVICE;
+        return;
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
+        g_dev_status = RL_ERR_NO_DEVICE;
+        return;
+    }
+    // The kernels are built for sm_103a only.
+    if (prop.major != 10 || prop.minor != 3) {
+        g_dev_status = RL_ERR_NO_DEVICE;
+        return;
+    }
+    g_num_sms = prop.multiProcessorCount;
+    // Keep freed blocks in the default pool so per-call workspaces are cheap.
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t threshold = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+    }
+    g_dev_status = RL_OK;
+}
+
+rl_status ensure_device() {
+    std::call_once(g_dev_once, init_device);
+    return g_dev_status;
+}
+
+int num_sms() {
+    ensure_device();
+    return g_num_sms > 0 ? g_num_sms : 152;
+}
+
+}  // namespace rl
+
+extern "C" {
+
+const char *rl_status_string(rl_status s) {
+    switch (s) {
+        case RL_OK: return "ok";
+        case RL_ERR_INVALID_ARG: return "invalid argument";
+        case RL_ERR_DECOMP_FAILURE: return "decomposition failure";
+        case RL_ERR_ALGEBRA_FAILURE: return "algebra failure";
+        case RL_ERR_DIV_BY_ZERO: return "division by zero (singular to working precision)";
+        case RL_ERR_SCALAR_CONVERSION: return "scalar conversion failure";
+        case RL_ERR_INVALID_PERMUTATION: return "invalid permutation";
+        case RL_ERR_SHAPE: return "dimension mismatch";
+        case RL_ERR_CUDA: return "CUDA error";
+        case RL_ERR_NO_DEVICE: return "no usable sm_103 GPU";
+        case RL_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case RL_ERR_TIMEOUT: return "device wait timed out";
+        case RL_ERR_NOT_CONVERGED: return "iterative refinement did not converge";
+        default: return "unknown status";
+    }
+}
+
+int rl_version(void) { return 100; }
+
+rl_status rl_device_check(void) { return rl::ensure_device(); }
+
+uint64_t rl_launch_count(void) { return rl::g_launches.load(std::memory_order_relaxed); }
+
+}  // extern "C"
