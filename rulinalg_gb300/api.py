@@ -102,6 +102,8 @@ def _mat(a, dtype=None) -> np.ndarray:
 
 def _row_stride(a: np.ndarray) -> int:
     """Row stride in elements of a 2D array whose rows are contiguous (MatrixSlice)."""
+    if a.size == 0:
+        return max(a.shape[1], 1)
     if a.shape[1] > 1 and a.strides[1] != a.itemsize:
         raise ValueError("rows must be contiguous")
     return a.strides[0] // a.itemsize if a.shape[0] > 1 else max(a.shape[1], 1)
@@ -120,9 +122,9 @@ def mat_mul(a, b) -> np.ndarray:
         raise TypeError("operands must share a dtype")
     if a.dtype not in (np.float32, np.float64):
         raise TypeError("GPU mat_mul covers f32 and f64")
-    if a.shape[1] > 1 and a.strides[1] != a.itemsize:
+    if a.size == 0 or (a.shape[1] > 1 and a.strides[1] != a.itemsize):
         a = np.ascontiguousarray(a)
-    if b.shape[1] > 1 and b.strides[1] != b.itemsize:
+    if b.size == 0 or (b.shape[1] > 1 and b.strides[1] != b.itemsize):
         b = np.ascontiguousarray(b)
     m, k = a.shape
     n = b.shape[1]

@@ -24,8 +24,8 @@ def golden():
 @pytest.fixture(scope="session")
 def rl():
     """The product library; built in-tree if it is missing (nvcc cross-compiles here)."""
-    from rulinalg_gb300 import build
-    build.build_library()
+    import __graft_entry__
+    __graft_entry__._build_module().build_library()
     import rulinalg_gb300
     return rulinalg_gb300
 
