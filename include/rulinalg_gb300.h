@@ -187,6 +187,24 @@ RL_API rl_status rl_dbatch_solve(rl_batch_plan *plan, const double *a, const dou
 RL_API rl_status rl_sbatch_solve(rl_batch_plan *plan, const float *a, const float *b, float *x, int32_t *info,
                           int32_t *iters, double *berr);
 
+/* ------------------------------------------------- solve without any allocation -- */
+/* No counterpart in the reference. For callers that cannot allocate device memory (a
+ * serving process that reserves all GPU memory at start-up and forbids allocation
+ * afterwards, or a host framework whose own pool owns the device memory): one f64 system
+ * A x = b with n <= 512, solved like an RL_PREC_MIXED batch of one (FP32 factor, FP64
+ * refinement, FP64 refactor fallback; kind = RL_KIND_LU or RL_KIND_CHOLESKY). Device
+ * pointers; asynchronous on `stream`; A is n x n row-major (row stride n). info / iters /
+ * berr receive one value each (iters, berr may be NULL).
+ * All scratch memory is one fixed array inside the library (about 3 MiB, held on every
+ * GPU that loads the library until the process exits); no cudaMalloc or other
+ * allocation happens. n > 512 returns RL_ERR_INVALID_ARG. The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) and sets the kernels'
+ * shared-memory limits, so make that first call before any stream capture. Calls share
+ * the array: calls that overlap on the GPU race on it and must be ordered by the caller
+ * (for example by issuing them on one stream). */
+RL_API rl_status rl_dsolve_mixed_noalloc_dev(size_t n, int kind, const double *a, const double *b, double *x,
+                                             int32_t *info, int32_t *iters, double *berr, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

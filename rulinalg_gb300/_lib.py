@@ -76,6 +76,7 @@ SIGNATURES = {
     "rl_sbatch_solve_dev": (st, [vp, vp, vp, vp, vp, vp, vp, vp]),
     "rl_dbatch_solve": (st, [vp, f64p, f64p, f64p, i32p, i32p, f64p]),
     "rl_sbatch_solve": (st, [vp, f32p, f32p, f32p, i32p, i32p, f64p]),
+    "rl_dsolve_mixed_noalloc_dev": (st, [sz, C.c_int, vp, vp, vp, vp, vp, vp, vp]),
 }
 
 for _name, (_res, _args) in SIGNATURES.items():
