@@ -187,6 +187,95 @@ RL_API rl_status rl_dbatch_solve(rl_batch_plan *plan, const double *a, const dou
 RL_API rl_status rl_sbatch_solve(rl_batch_plan *plan, const float *a, const float *b, float *x, int32_t *info,
                           int32_t *iters, double *berr);
 
+/* ---------------------------------------------- mixed-precision single systems -- */
+/* One (typically large) f64 system A X = B, n x n, nrhs columns (row-major, strides).
+ * The replaced reference call is `PartialPivLu::decompose(a)?.solve(b)` (lu.rs:163-244)
+ * or `Cholesky::decompose(a)?.solve(b)` (cholesky.rs:116-202) per column.
+ * rl_dsolve_mixed*: FP32 factor on the GPU (kind = RL_KIND_LU / RL_KIND_CHOLESKY), FP64
+ * residual, update and backward-error stopping test (||r|| <= sqrt(n) u ||A|| ||x||);
+ * when plain refinement stalls or diverges, GMRES-IR (restarted FP64 GMRES
+ * left-preconditioned by the FP32 factors); when that fails too, or the FP32 factor
+ * breaks down, an FP64 refactor. rl_dsolve_fp64_dev: the plain all-FP64 GPU solve.
+ * info (may be NULL) reports the refinement steps, GMRES iterations, the path taken and
+ * the max normwise backward error over the columns. The _dev forms take device
+ * pointers and synchronise the stream (the host reads the stopping test). */
+#define RL_PATH_REFINEMENT 0
+#define RL_PATH_GMRES 1
+#define RL_PATH_FP64 2
+typedef struct rl_solve_info {
+    int32_t iters;
+    int32_t gmres_iters;
+    int32_t path;
+    int32_t reserved;
+    double berr;
+} rl_solve_info;
+RL_API rl_status rl_dsolve_mixed_dev(size_t n, size_t nrhs, int kind, const double *a, size_t lda, const double *b,
+                                     size_t ldb, double *x, size_t ldx, rl_solve_info *info, void *stream);
+RL_API rl_status rl_dsolve_mixed(size_t n, size_t nrhs, int kind, const double *a, size_t lda, const double *b,
+                                 size_t ldb, double *x, size_t ldx, rl_solve_info *info);
+RL_API rl_status rl_dsolve_fp64_dev(size_t n, size_t nrhs, int kind, const double *a, size_t lda, const double *b,
+                                    size_t ldb, double *x, size_t ldx, rl_solve_info *info, void *stream);
+
+/* ---------------------------------------------------------------------- serving -- */
+/* A request loop in front of the GPU solvers (no counterpart in the reference, which is
+ * a single-threaded library): clients submit requests from any thread and wait on
+ * tickets; worker threads with their own CUDA streams batch the small LU / Cholesky
+ * requests that are waiting into one mixed-precision launch (continuous batching), run
+ * the others alone, keep factors resident on request (re-solves with new right-hand
+ * sides reuse them), and admit work only while its device-memory footprint fits the
+ * budget. Answers are f64-accurate (backward error as for RL_PREC_MIXED); QR least
+ * squares is FP64 Householder QR of [A | b]. Host buffers a, b, x must stay valid until
+ * the ticket completes. */
+#define RL_REQ_LU 0
+#define RL_REQ_CHOLESKY 1
+#define RL_REQ_LSTSQ 2
+#define RL_REQ_RESOLVE 3
+typedef struct rl_server rl_server;
+typedef struct rl_server_config {
+    size_t hbm_budget_bytes; /* 0: 80% of the free device memory after start-up */
+    int workers;             /* worker threads / CUDA streams (0: 4) */
+    int max_batch;           /* systems per batched launch (0: 4096) */
+    int small_n;             /* largest n sent to the batched kernel (0: 512) */
+} rl_server_config;
+typedef struct rl_request {
+    int kind;        /* RL_REQ_* */
+    int retain;      /* LU / Cholesky: keep the factor resident; its handle comes back in rl_result.factor */
+    uint64_t factor; /* RL_REQ_RESOLVE: handle of a resident factor */
+    size_t m, n;     /* A is m x n (m = n, or 0, except for least squares) */
+    const double *a; /* host, row-major m x n (unused for RL_REQ_RESOLVE) */
+    const double *b; /* host, m entries */
+    double *x;       /* host, n entries, written on completion */
+} rl_request;
+typedef struct rl_result {
+    rl_status status;
+    int32_t iters;     /* refinement steps */
+    int32_t path;      /* RL_PATH_* */
+    int32_t reserved;
+    double berr;       /* normwise backward error (0 for least squares) */
+    uint64_t factor;   /* resident factor handle (retain / re-solve) */
+    double queue_us;   /* submit -> a worker took it */
+    double latency_us; /* submit -> result on the host */
+} rl_result;
+typedef struct rl_server_stats {
+    uint64_t submitted, completed, failed, batches, batched_requests;
+    uint64_t bytes_in_use, bytes_peak, bytes_budget, resident_factors;
+    double p50_us, p99_us, mean_us, solves_per_s;
+} rl_server_stats;
+RL_API rl_status rl_server_create(const rl_server_config *cfg, rl_server **server);
+/* Non-blocking; RL_ERR_OUT_OF_MEMORY when the request can never fit the budget. */
+RL_API rl_status rl_server_submit(rl_server *server, const rl_request *req, uint64_t *ticket);
+/* Blocks until the ticket completes (timeout_s < 0: no limit); the ticket is consumed. */
+RL_API rl_status rl_server_wait(rl_server *server, uint64_t ticket, double timeout_s, rl_result *result);
+RL_API rl_status rl_server_release_factor(rl_server *server, uint64_t factor);
+RL_API rl_status rl_server_stats_get(rl_server *server, rl_server_stats *stats);
+RL_API rl_status rl_server_reset_stats(rl_server *server);
+/* Load replay: submits reqs[i] at arrival_s[i] seconds after the call (a Poisson trace,
+ * say), then waits for all of them; results[i] receives each outcome. */
+RL_API rl_status rl_server_replay(rl_server *server, size_t count, const double *arrival_s, const rl_request *reqs,
+                                  rl_result *results);
+/* Drains the admitted requests, releases resident factors and stops the workers. */
+RL_API rl_status rl_server_destroy(rl_server *server);
+
 /* ------------------------------------------------- solve without any allocation -- */
 /* No counterpart in the reference. For callers that cannot allocate device memory (a
  * serving process that reserves all GPU memory at start-up and forbids allocation

@@ -77,7 +77,49 @@ SIGNATURES = {
     "rl_dbatch_solve": (st, [vp, f64p, f64p, f64p, i32p, i32p, f64p]),
     "rl_sbatch_solve": (st, [vp, f32p, f32p, f32p, i32p, i32p, f64p]),
     "rl_dsolve_mixed_noalloc_dev": (st, [sz, C.c_int, vp, vp, vp, vp, vp, vp, vp]),
+    "rl_dsolve_mixed_dev": (st, [sz, sz, C.c_int, vp, sz, vp, sz, vp, sz, vp, vp]),
+    "rl_dsolve_mixed": (st, [sz, sz, C.c_int, f64p, sz, f64p, sz, f64p, sz, vp]),
+    "rl_dsolve_fp64_dev": (st, [sz, sz, C.c_int, vp, sz, vp, sz, vp, sz, vp, vp]),
+    "rl_server_create": (st, [vp, C.POINTER(vp)]),
+    "rl_server_submit": (st, [vp, vp, C.POINTER(C.c_uint64)]),
+    "rl_server_wait": (st, [vp, C.c_uint64, C.c_double, vp]),
+    "rl_server_release_factor": (st, [vp, C.c_uint64]),
+    "rl_server_stats_get": (st, [vp, vp]),
+    "rl_server_reset_stats": (st, [vp]),
+    "rl_server_replay": (st, [vp, sz, vp, vp, vp]),
+    "rl_server_destroy": (st, [vp]),
 }
+
+
+class ServerConfig(C.Structure):
+    """rl_server_config"""
+    _fields_ = [("hbm_budget_bytes", C.c_size_t), ("workers", C.c_int), ("max_batch", C.c_int), ("small_n", C.c_int)]
+
+
+class Request(C.Structure):
+    """rl_request"""
+    _fields_ = [("kind", C.c_int), ("retain", C.c_int), ("factor", C.c_uint64), ("m", C.c_size_t), ("n", C.c_size_t),
+                ("a", C.c_void_p), ("b", C.c_void_p), ("x", C.c_void_p)]
+
+
+class Result(C.Structure):
+    """rl_result"""
+    _fields_ = [("status", C.c_int), ("iters", C.c_int32), ("path", C.c_int32), ("reserved", C.c_int32),
+                ("berr", C.c_double), ("factor", C.c_uint64), ("queue_us", C.c_double), ("latency_us", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    """rl_server_stats"""
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64), ("batches", C.c_uint64),
+                ("batched_requests", C.c_uint64), ("bytes_in_use", C.c_uint64), ("bytes_peak", C.c_uint64),
+                ("bytes_budget", C.c_uint64), ("resident_factors", C.c_uint64), ("p50_us", C.c_double),
+                ("p99_us", C.c_double), ("mean_us", C.c_double), ("solves_per_s", C.c_double)]
+
+
+class SolveInfo(C.Structure):
+    """rl_solve_info"""
+    _fields_ = [("iters", C.c_int32), ("gmres_iters", C.c_int32), ("path", C.c_int32), ("reserved", C.c_int32),
+                ("berr", C.c_double)]
 
 for _name, (_res, _args) in SIGNATURES.items():
     _fn = getattr(lib, _name)

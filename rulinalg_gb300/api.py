@@ -346,3 +346,29 @@ def det(matrix) -> float:
     out = np.zeros(1, dtype=a.dtype)
     _check(_fn(_prefix(a), "matrix_det")(n, _ptr(a), max(n, 1), _ptr(out)))
     return out[0].item()
+
+
+PATHS = {0: "refinement", 1: "gmres-ir", 2: "fp64"}
+
+
+def solve_mixed(matrix, b, kind: str = "lu"):
+    """f64 solve through the mixed-precision single-system solver (FP32 factor, FP64
+    refinement, GMRES-IR, FP64 refactor as needed). Returns (x, info) where info has
+    iters, gmres_iters, path and berr (max normwise backward error over the columns)."""
+    from ._lib import SolveInfo
+    a = np.ascontiguousarray(matrix, dtype=np.float64)
+    n = a.shape[0]
+    if a.shape != (n, n):
+        raise RulinalgPanic("Matrix must be square.")
+    bb = np.ascontiguousarray(b, dtype=np.float64)
+    vec = bb.ndim == 1
+    bb = bb.reshape(n, -1)
+    nrhs = bb.shape[1]
+    x = np.zeros_like(bb)
+    info = SolveInfo()
+    k = 1 if kind == "cholesky" else 0
+    _check(lib.rl_dsolve_mixed(n, nrhs, k, _ptr(a), max(n, 1), _ptr(bb), max(nrhs, 1), _ptr(x), max(nrhs, 1),
+                               C.byref(info)))
+    out = {"iters": info.iters, "gmres_iters": info.gmres_iters, "path": PATHS.get(info.path, info.path),
+           "berr": info.berr}
+    return (x[:, 0] if vec else x), out

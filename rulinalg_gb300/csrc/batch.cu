@@ -202,7 +202,8 @@ rl_status plan_init(rl_batch_plan *p, size_t count, const int32_t *n, const uint
     RL_TRY(upload(p->d_order, order, s));
     RL_TRY_CUDA(cudaMalloc(&p->d_counters, 4 * sizeof(int)));
     RL_TRY_CUDA(cudaMalloc(&p->d_fb_list, std::max<size_t>(1, count) * sizeof(int)));
-    p->work_stride = std::max(1LL, (long long)p->max_n * p->max_n);
+    const long long npad = (p->max_n + 3) & ~3;  // slot row stride rounded up to 4
+    p->work_stride = std::max(4LL, npad * npad);
     if (precision == RL_PREC_MIXED) {
         p->smem = cta_smem_bytes<float>();
         RL_TRY((occupancy_grid<double, float, true>(p->smem, p->grid)));

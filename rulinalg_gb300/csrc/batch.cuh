@@ -21,7 +21,7 @@ struct BatchDesc {
     int *fb_list;            // mixed precision: systems handed to the FP64 pass
     int *fb_count;
     void *work;              // per-CTA factor workspace slots
-    long long work_stride;   // elements per slot (>= 512 * 512)
+    long long work_stride;   // elements per slot (>= ldw * n, ldw = n rounded up to 4)
     int *info;               // per-system status
     int *iters;              // refinement steps (-1: solved by the FP64 fallback pass)
     double *berr;            // normwise backward error ||b - Ax|| / (||A|| ||x|| + ||b||), inf-norms
@@ -67,11 +67,13 @@ __device__ void batch_solve_one(const BatchDesc &d, int sys, const TI *__restric
         __syncthreads();
         return;
     }
-    // Working copy in the factor type; ||A||_inf from the same pass.
+    // Working copy in the factor type (row stride rounded up to 4 elements so that the
+    // trailing updates use 128-bit accesses); ||A||_inf from the same pass.
+    const int ldw = (n + 3) & ~3;
     double rowmax = 0.0;
     for (int i = warp; i < n; i += CTA_WARPS) {
         const TI *row = Ai + (long long)i * n;
-        TF *wrow = W + (long long)i * n;
+        TF *wrow = W + (long long)i * ldw;
         TF s = TF(0);
         for (int j = lane; j < n; j += 32) {
             const TF v = (TF)row[j];
@@ -87,11 +89,11 @@ __device__ void batch_solve_one(const BatchDesc &d, int sys, const TI *__restric
     const double bnorm = block_max(bm, S);
 
     const TF tiny = MIXED ? TF(FLT_MIN) : Eps<TF>::value;
-    int st = kind ? cta_chol_factor<TF>(W, n, n, S, tiny) : cta_lu_factor<TF>(W, n, n, S, tiny);
+    int st = kind ? cta_chol_factor<TF>(W, ldw, n, S, tiny) : cta_lu_factor<TF>(W, ldw, n, S, tiny);
     if (st == RL_OK) {
         for (int i = tid; i < n; i += CTA_THREADS) S.w[i] = (TF)bi[i];
         __syncthreads();
-        st = cta_factor_solve<TF>(W, n, n, kind, S, tiny);
+        st = cta_factor_solve<TF>(W, ldw, n, kind, S, tiny);
     }
     if (st != RL_OK) {
         if (MIXED)
@@ -139,7 +141,7 @@ __device__ void batch_solve_one(const BatchDesc &d, int sys, const TI *__restric
         const double scale = 1.0 / rn;
         for (int i = tid; i < n; i += CTA_THREADS) S.w[i] = (TF)(S.r[i] * scale);
         __syncthreads();
-        if (cta_factor_solve<TF>(W, n, n, kind, S, tiny) != RL_OK) break;
+        if (cta_factor_solve<TF>(W, ldw, n, kind, S, tiny) != RL_OK) break;
         for (int i = tid; i < n; i += CTA_THREADS) S.x[i] = fma(rn, (double)S.w[i], S.x[i]);
         __syncthreads();
     }
@@ -153,7 +155,7 @@ __device__ void batch_solve_one(const BatchDesc &d, int sys, const TI *__restric
 }
 
 template <class TI, class TF, bool MIXED>
-__global__ void __launch_bounds__(CTA_THREADS) batch_solve_kernel(BatchDesc d, const TI *A, const TI *B, TI *X) {
+__global__ void __launch_bounds__(CTA_THREADS, 2) batch_solve_kernel(BatchDesc d, const TI *A, const TI *B, TI *X) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CtaSmem<TF> &S = *reinterpret_cast<CtaSmem<TF> *>(smem_raw);
     TF *W = static_cast<TF *>(d.work) + (long long)blockIdx.x * d.work_stride;
@@ -173,7 +175,7 @@ __global__ void __launch_bounds__(CTA_THREADS) batch_solve_kernel(BatchDesc d, c
 // Factor one matrix in place. kind 0: LU (ipiv receives LAPACK-style pivots),
 // 1: Cholesky. status[0] receives the result.
 template <class T>
-__global__ void __launch_bounds__(CTA_THREADS)
+__global__ void __launch_bounds__(CTA_THREADS, 2)
     factor_one_kernel(T *A, int lda, int n, int kind, int *ipiv, int *status, T tiny) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CtaSmem<T> &S = *reinterpret_cast<CtaSmem<T> *>(smem_raw);

@@ -34,7 +34,7 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
     return v;
 }
 
-__device__ bool grid_barrier(unsigned *ctr, unsigned target, int *err) {
+static __device__ bool grid_barrier(unsigned *ctr, unsigned target, int *err) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -77,7 +77,7 @@ struct PanelSync {
 // ties), swaps, scales and updates its rows. ipiv receives k0-based global pivots.
 // cand: 2 slots x G x (2 + NB) values, rowj: 2 slots x NB values.
 template <class T>
-__global__ void __launch_bounds__(256) lu_panel_kernel(T *P, long long lda, int mrows, int kb, int k0, int rows_per,
+static __global__ void __launch_bounds__(256) lu_panel_kernel(T *P, long long lda, int mrows, int kb, int k0, int rows_per,
                                                        int *ipiv, T *cand, T *rowj, PanelSync *sync, T tiny) {
     constexpr int NB = PanelNB<T>::value;
     constexpr int LDR = NB + 1;
@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(256) lu_panel_kernel(T *P, long long lda, int 
 // in CTA order after a grid barrier. Two barriers per column. tau receives kb values.
 // part: 2 slots x G x (1 + NB) partial sums; x0buf: 2 slots.
 template <class T>
-__global__ void __launch_bounds__(256) qr_panel_kernel(T *P, long long lda, int mrows, int kb, int rows_per, T *tau,
+static __global__ void __launch_bounds__(256) qr_panel_kernel(T *P, long long lda, int mrows, int kb, int rows_per, T *tau,
                                                        T *part, T *x0buf, PanelSync *sync) {
     constexpr int NB = PanelNB<T>::value;
     constexpr int LDR = NB + 1;
@@ -272,7 +272,7 @@ __global__ void __launch_bounds__(256) qr_panel_kernel(T *P, long long lda, int 
 // Applies ipiv[j0..j1) (global rows; step j swaps rows j and ipiv[j]) to the columns
 // [0, c_skip0) and [c_skip1, ncols) of A. Thread per column, swaps in order.
 template <class T>
-__global__ void laswp_kernel(T *A, long long lda, int ncols, int c_skip0, int c_skip1, const int *ipiv, int j0,
+static __global__ void laswp_kernel(T *A, long long lda, int ncols, int c_skip0, int c_skip1, const int *ipiv, int j0,
                              int j1) {
     const int nother = ncols - (c_skip1 - c_skip0);
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -296,7 +296,7 @@ __global__ void laswp_kernel(T *A, long long lda, int ncols, int c_skip0, int c_
 // 3: D^T with D lower (L^T). One thread per right-hand-side column. |d_ii| < tiny
 // (modes 1-3) records RL_ERR_DIV_BY_ZERO in status.
 template <class T>
-__global__ void __launch_bounds__(64) trsm_diag_kernel(const T *D, long long ldd, int bs, T *Y, long long ldy,
+static __global__ void __launch_bounds__(64) trsm_diag_kernel(const T *D, long long ldd, int bs, T *Y, long long ldy,
                                                        int nrhs, int mode, int *status, T tiny) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T (*Ds)[65] = reinterpret_cast<T (*)[65]>(smem_raw);             // 64 x 65
@@ -343,7 +343,7 @@ __global__ void __launch_bounds__(64) trsm_diag_kernel(const T *D, long long ldd
 // Row-wise solve X D^T = Y for the rows of Y (m x bs, stride ldy), D lower bs x bs:
 // the Cholesky panel L21 = A21 L11^-T. Thread per row.
 template <class T>
-__global__ void __launch_bounds__(128) trsm_right_lt_kernel(const T *D, long long ldd, int bs, T *Y, long long ldy,
+static __global__ void __launch_bounds__(128) trsm_right_lt_kernel(const T *D, long long ldd, int bs, T *Y, long long ldy,
                                                             int m) {
     __shared__ T Ds[64][65];
     for (int idx = threadIdx.x; idx < bs * bs; idx += blockDim.x) {
@@ -377,7 +377,7 @@ __global__ void __launch_bounds__(128) trsm_right_lt_kernel(const T *D, long lon
 // V (mrows x kb, row stride kb) = the panel's reflectors with the implicit unit diagonal
 // and zeros above it.
 template <class T>
-__global__ void extract_v_kernel(const T *P, long long lda, int mrows, int kb, T *V) {
+static __global__ void extract_v_kernel(const T *P, long long lda, int mrows, int kb, T *V) {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long long)mrows * kb) return;
     const int r = (int)(idx / kb), c = (int)(idx - (long long)r * kb);
@@ -387,7 +387,7 @@ __global__ void extract_v_kernel(const T *P, long long lda, int mrows, int kb, T
 // T factor of H_0 ... H_{kb-1} = I - V T V^T (upper triangular, kb x kb) from the
 // Gram matrix Gm = V^T V and tau: T[j][j] = tau_j, T[0:j, j] = -tau_j T[0:j, 0:j] Gm[0:j, j].
 template <class T>
-__global__ void larft_kernel(const T *Gm, const T *tau, int kb, T *Tm) {
+static __global__ void larft_kernel(const T *Gm, const T *tau, int kb, T *Tm) {
     __shared__ T w[64];
     const int t = threadIdx.x;
     for (int idx = t; idx < kb * kb; idx += blockDim.x) Tm[idx] = T(0);
@@ -408,7 +408,7 @@ __global__ void larft_kernel(const T *Gm, const T *tau, int kb, T *Tm) {
 
 // Identity-like start for first_k_columns: Q (m x k) = I[:, 0:k].
 template <class T>
-__global__ void eye_kernel(T *Q, long long ldq, int m, int k) {
+static __global__ void eye_kernel(T *Q, long long ldq, int m, int k) {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long long)m * k) return;
     const int r = (int)(idx / k), c = (int)(idx - (long long)r * k);
@@ -417,7 +417,7 @@ __global__ void eye_kernel(T *Q, long long ldq, int m, int k) {
 
 // Gathers rows: Y[perm[i]][:] = B[i][:] (the reference's P * b, applied to nrhs columns).
 template <class T>
-__global__ void permute_rows_kernel(const T *B, long long ldb, T *Y, long long ldy, int n, int nrhs,
+static __global__ void permute_rows_kernel(const T *B, long long ldb, T *Y, long long ldy, int n, int nrhs,
                                     const uint64_t *perm) {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long long)n * nrhs) return;
@@ -428,7 +428,7 @@ __global__ void permute_rows_kernel(const T *B, long long ldb, T *Y, long long l
 // det helpers: sequential fold of the diagonal in row order (the reference's fold), and
 // the parity of a stored permutation by cycle resolution (permutation_matrix.rs:479-509).
 template <class T>
-__global__ void det_kernel(const T *A, long long lda, int n, const uint64_t *perm, uint64_t *scratch, int square,
+static __global__ void det_kernel(const T *A, long long lda, int n, const uint64_t *perm, uint64_t *scratch, int square,
                            T *out) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     T d = T(1);

@@ -1,0 +1,341 @@
+// Device-side orchestration shared by the host entry points: blocked factorisations
+// (LU, Cholesky, Householder QR), Q formation, triangular solves and factor solves on
+// buffers already on the GPU. Every function launches on the given stream; the ones
+// that return a numerical status synchronise to read it.
+#pragma once
+
+#include <algorithm>
+#include <type_traits>
+#include <vector>
+
+#include "batch.cuh"
+#include "dense.cuh"
+#include "gemm.cuh"
+#include "mixed.cuh"
+
+namespace rl {
+
+
+template <class T>
+inline rl_status read_status(const int *dstatus, cudaStream_t s) {
+    int h = 0;
+    RL_TRY_CUDA(cudaMemcpyAsync(&h, dstatus, sizeof(int), cudaMemcpyDeviceToHost, s));
+    RL_TRY_CUDA(cudaStreamSynchronize(s));
+    return h;
+}
+
+template <class K>
+inline rl_status set_smem(K kern, size_t bytes) {
+    static_assert(std::is_pointer<K>::value, "kernel pointer");
+    if (bytes > 48 * 1024)
+        RL_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    return RL_OK;
+}
+
+// One CTA factors a matrix with n <= CTA_NMAX; kind 0 LU (ipiv out), 1 Cholesky.
+template <class T>
+rl_status factor_small(T *A, long long lda, int n, int kind, int *ipiv, cudaStream_t s, T tiny = Eps<T>::value) {
+    DevBuf<int> st;
+    RL_TRY(st.alloc(1, s));
+    RL_TRY_CUDA(cudaMemsetAsync(st.p, 0, sizeof(int), s));
+    const size_t smem = cta_smem_bytes<T>();
+    RL_TRY(set_smem(factor_one_kernel<T>, smem));
+    RL_LAUNCH(factor_one_kernel<T>, 1, CTA_THREADS, smem, s, A, (int)lda, n, kind, ipiv, st.p, tiny);
+    return read_status<T>(st.p, s);
+}
+
+// Cooperative panel geometry: G CTAs of rows_per rows each.
+template <class T>
+void panel_geometry(int mrows, int &G, int &rows_per) {
+    const int target = std::is_same<T, double>::value ? 64 : 128;
+    G = std::max(1, std::min(num_sms(), (mrows + target - 1) / target));
+    rows_per = (mrows + G - 1) / G;
+}
+
+template <class T>
+rl_status launch_coop(void *kern, int G, size_t smem, void **args, cudaStream_t s) {
+    RL_TRY_CUDA(cudaLaunchCooperativeKernel(kern, dim3(G), dim3(256), args, smem, s));
+    count_launch();
+    return RL_OK;
+}
+
+// Blocked right-looking LU for any n: cooperative panel, row swaps, U12 solve, GEMM.
+template <class T>
+rl_status lu_factor_dev(T *A, long long lda, int n, int *ipiv, cudaStream_t s, T tiny = Eps<T>::value) {
+    if (n <= 0) return RL_OK;
+    if (n <= CTA_NMAX) return factor_small<T>(A, lda, n, 0, ipiv, s, tiny);
+    constexpr int NB = PanelNB<T>::value;
+    int Gmax, rp;
+    panel_geometry<T>(n, Gmax, rp);
+    if ((size_t)rp * (NB + 1) * sizeof(T) > 200 * 1024) return RL_ERR_INVALID_ARG;  // n beyond ~50k
+    DevBuf<T> cand, rowj;
+    DevBuf<PanelSync> sync;
+    RL_TRY(cand.alloc((size_t)2 * Gmax * (2 + NB), s));
+    RL_TRY(rowj.alloc(2 * NB, s));
+    RL_TRY(sync.alloc(1, s));
+    auto pk = lu_panel_kernel<T>;
+    RL_TRY(set_smem(pk, 200 * 1024));
+    const size_t tsm = sizeof(T) * (64 * 65 + 64 * 64);
+    RL_TRY(set_smem(trsm_diag_kernel<T>, tsm));
+    for (int k0 = 0; k0 < n; k0 += NB) {
+        const int kb = std::min(NB, n - k0), mrows = n - k0;
+        int G, rows_per;
+        panel_geometry<T>(mrows, G, rows_per);
+        const size_t smem = ((size_t)rows_per * (NB + 1) + NB) * sizeof(T);
+        RL_TRY_CUDA(cudaMemsetAsync(sync.p, 0, sizeof(PanelSync), s));
+        T *P = A + (long long)k0 * lda + k0;
+        int *ip = ipiv + k0;
+        void *args[] = {&P, &lda, (void *)&mrows, (void *)&kb, &k0, &rows_per, &ip, &cand.p, &rowj.p, &sync.p, &tiny};
+        RL_TRY(launch_coop<T>((void *)pk, G, smem, args, s));
+        int err = 0;
+        RL_TRY_CUDA(cudaMemcpyAsync(&err, &sync.p->err, sizeof(int), cudaMemcpyDeviceToHost, s));
+        RL_TRY_CUDA(cudaStreamSynchronize(s));
+        if (err) return err;
+        const int nother = n - kb;
+        if (nother > 0)
+            RL_LAUNCH(laswp_kernel<T>, ceil_div(nother, 256), 256, 0, s, A, lda, n, k0, k0 + kb, ipiv, k0, k0 + kb);
+        const int n2 = n - k0 - kb;
+        if (n2 > 0) {
+            DevBuf<int> st;
+            RL_TRY(st.alloc(1, s));
+            RL_TRY_CUDA(cudaMemsetAsync(st.p, 0, sizeof(int), s));
+            RL_LAUNCH(trsm_diag_kernel<T>, ceil_div(n2, 64), 64, tsm, s, P, lda, kb, P + kb, lda, n2, 0, st.p, tiny);
+            RL_TRY((gemm<T, false, false>(n2, n2, kb, T(-1), P + (long long)kb * lda, lda, P + kb, lda, T(1),
+                                         P + (long long)kb * lda + kb, lda, s)));
+        }
+    }
+    return RL_OK;
+}
+
+// Blocked right-looking Cholesky: diagonal block by one CTA, L21 = A21 L11^-T, SYRK.
+template <class T>
+rl_status chol_factor_dev(T *A, long long lda, int n, cudaStream_t s, T tiny = Eps<T>::value) {
+    if (n <= 0) return RL_OK;
+    if (n <= CTA_NMAX) return factor_small<T>(A, lda, n, 1, nullptr, s, tiny);
+    constexpr int NB = PanelNB<T>::value;
+    for (int k0 = 0; k0 < n; k0 += NB) {
+        const int kb = std::min(NB, n - k0), mrows = n - k0;
+        T *P = A + (long long)k0 * lda + k0;
+        RL_TRY(factor_small<T>(P, lda, kb, 1, nullptr, s, tiny));
+        const int m2 = mrows - kb;
+        if (m2 > 0) {
+            RL_LAUNCH(trsm_right_lt_kernel<T>, ceil_div(m2, 128), 128, 0, s, P, lda, kb, P + (long long)kb * lda, lda,
+                      m2);
+            T *L21 = P + (long long)kb * lda;
+            RL_TRY((gemm<T, false, true, true>(m2, m2, kb, T(-1), L21, lda, L21, lda, T(1), L21 + kb, lda, s)));
+        }
+    }
+    return RL_OK;
+}
+
+// Blocked Householder QR with compact-WY trailing updates; nrefl reflectors
+// (min(m, n) for a plain QR; n for the augmented least-squares matrix).
+template <class T>
+rl_status qr_factor_dev(T *A, long long lda, int m, int n, int nrefl, T *tau, cudaStream_t s) {
+    if (nrefl <= 0) return RL_OK;
+    constexpr int NB = PanelNB<T>::value;
+    int Gmax, rp;
+    panel_geometry<T>(m, Gmax, rp);
+    if ((size_t)rp * (NB + 1) * sizeof(T) > 200 * 1024) return RL_ERR_INVALID_ARG;
+    DevBuf<T> part, x0buf, V, Gm, Tm, W1, W2;
+    DevBuf<PanelSync> sync;
+    RL_TRY(part.alloc((size_t)2 * Gmax * (1 + NB), s));
+    RL_TRY(x0buf.alloc(2, s));
+    RL_TRY(sync.alloc(1, s));
+    RL_TRY(V.alloc((size_t)m * NB, s));
+    RL_TRY(Gm.alloc(NB * NB, s));
+    RL_TRY(Tm.alloc(NB * NB, s));
+    RL_TRY(W1.alloc((size_t)NB * std::max(1, n), s));
+    RL_TRY(W2.alloc((size_t)NB * std::max(1, n), s));
+    auto pk = qr_panel_kernel<T>;
+    RL_TRY(set_smem(pk, 200 * 1024));
+    for (int k0 = 0; k0 < nrefl; k0 += NB) {
+        const int kb = std::min(NB, nrefl - k0), mrows = m - k0;
+        int G, rows_per;
+        panel_geometry<T>(mrows, G, rows_per);
+        const size_t smem = ((size_t)rows_per * (NB + 1) + NB) * sizeof(T);
+        RL_TRY_CUDA(cudaMemsetAsync(sync.p, 0, sizeof(PanelSync), s));
+        T *P = A + (long long)k0 * lda + k0;
+        T *tk = tau + k0;
+        void *args[] = {&P, &lda, (void *)&mrows, (void *)&kb, &rows_per, &tk, &part.p, &x0buf.p, &sync.p};
+        RL_TRY(launch_coop<T>((void *)pk, G, smem, args, s));
+        int err = 0;
+        RL_TRY_CUDA(cudaMemcpyAsync(&err, &sync.p->err, sizeof(int), cudaMemcpyDeviceToHost, s));
+        RL_TRY_CUDA(cudaStreamSynchronize(s));
+        if (err) return err;
+        const int n2 = n - k0 - kb;
+        if (n2 <= 0) continue;
+        const long long mk = (long long)mrows * kb;
+        RL_LAUNCH(extract_v_kernel<T>, (int)((mk + 255) / 256), 256, 0, s, P, lda, mrows, kb, V.p);
+        RL_TRY((gemm<T, true, false>(kb, kb, mrows, T(1), V.p, kb, V.p, kb, T(0), Gm.p, kb, s)));
+        RL_LAUNCH(larft_kernel<T>, 1, 64, 0, s, Gm.p, tk, kb, Tm.p);
+        T *A2 = P + kb;
+        RL_TRY((gemm<T, true, false>(kb, n2, mrows, T(1), V.p, kb, A2, lda, T(0), W1.p, n2, s)));
+        RL_TRY((gemm<T, true, false>(kb, n2, kb, T(1), Tm.p, kb, W1.p, n2, T(0), W2.p, n2, s)));
+        RL_TRY((gemm<T, false, false>(mrows, n2, kb, T(-1), V.p, kb, W2.p, n2, T(1), A2, lda, s)));
+    }
+    return RL_OK;
+}
+
+// Q[:, 0:k] of a compact QR (HouseholderComposition::first_k_columns): reflector panels
+// applied in reverse order to I[:, 0:k], each as Q2 -= V (T (V^T Q2)).
+template <class T>
+rl_status qr_first_k_dev(const T *QR, long long lda, int m, int n, const T *tau, int k, T *Q, long long ldq,
+                         cudaStream_t s) {
+    if (m <= 0 || k <= 0) return RL_OK;
+    constexpr int NB = PanelNB<T>::value;
+    const long long mk = (long long)m * k;
+    RL_LAUNCH(eye_kernel<T>, (int)((mk + 255) / 256), 256, 0, s, Q, ldq, m, k);
+    const int jmax = std::min(std::min(m, n), k);
+    if (jmax <= 0) return RL_OK;
+    DevBuf<T> V, Gm, Tm, W1, W2;
+    RL_TRY(V.alloc((size_t)m * NB, s));
+    RL_TRY(Gm.alloc(NB * NB, s));
+    RL_TRY(Tm.alloc(NB * NB, s));
+    RL_TRY(W1.alloc((size_t)NB * k, s));
+    RL_TRY(W2.alloc((size_t)NB * k, s));
+    for (int k0 = ((jmax - 1) / NB) * NB; k0 >= 0; k0 -= NB) {
+        const int kb = std::min(NB, jmax - k0), mrows = m - k0, nc = k - k0;
+        const T *P = QR + (long long)k0 * lda + k0;
+        const long long mkb = (long long)mrows * kb;
+        RL_LAUNCH(extract_v_kernel<T>, (int)((mkb + 255) / 256), 256, 0, s, P, lda, mrows, kb, V.p);
+        RL_TRY((gemm<T, true, false>(kb, kb, mrows, T(1), V.p, kb, V.p, kb, T(0), Gm.p, kb, s)));
+        RL_LAUNCH(larft_kernel<T>, 1, 64, 0, s, Gm.p, tau + k0, kb, Tm.p);
+        T *Q2 = Q + (long long)k0 * ldq + k0;
+        RL_TRY((gemm<T, true, false>(kb, nc, mrows, T(1), V.p, kb, Q2, ldq, T(0), W1.p, nc, s)));
+        RL_TRY((gemm<T, false, false>(kb, nc, kb, T(1), Tm.p, kb, W1.p, nc, T(0), W2.p, nc, s)));
+        RL_TRY((gemm<T, false, false>(mrows, nc, kb, T(-1), V.p, kb, W2.p, nc, T(1), Q2, ldq, s)));
+    }
+    return RL_OK;
+}
+
+// Blocked triangular solve op(A) X = Y in place (A n x n, Y n x nrhs).
+// mode 0: unit lower, 1: lower, 2: upper, 3: L^T with L lower. |d_ii| < eps is
+// recorded as RL_ERR_DIV_BY_ZERO in *dstatus.
+template <class T>
+rl_status tri_solve_dev(const T *A, long long lda, int n, T *Y, long long ldy, int nrhs, int mode, int *dstatus,
+                        cudaStream_t s, T tiny = Eps<T>::value) {
+    if (n <= 0 || nrhs <= 0) return RL_OK;
+    constexpr int NB = 64;
+    if (nrhs <= 8) {
+        // Few right-hand sides: warp-per-column diagonal blocks and warp-per-row GEMV
+        // updates (a GEMM tile would waste all but nrhs of its columns).
+        const int wpb = 8, gridr = std::max(1, std::min(4 * num_sms(), ceil_div(n, wpb)));
+        if (mode == 0 || mode == 1) {
+            for (int b0 = 0; b0 < n; b0 += NB) {
+                const int bs = std::min(NB, n - b0), rest = n - b0 - bs;
+                T *Yb = Y + (long long)b0 * ldy;
+                RL_LAUNCH(trsv_diag_kernel<T>, 1, 256, 0, s, A + (long long)b0 * lda + b0, lda, bs, Yb, ldy, nrhs, mode,
+                          dstatus, tiny);
+                if (rest > 0)
+                    RL_LAUNCH(gemv_update_kernel<T>, std::min(gridr, ceil_div(rest, wpb)), 32 * wpb, 0, s,
+                              A + (long long)(b0 + bs) * lda + b0, lda, rest, bs, Yb, ldy, Yb + (long long)bs * ldy,
+                              nrhs, false);
+            }
+        } else {
+            for (int b1 = n; b1 > 0; b1 -= NB) {
+                const int b0 = std::max(0, b1 - NB), bs = b1 - b0;
+                T *Yb = Y + (long long)b0 * ldy;
+                RL_LAUNCH(trsv_diag_kernel<T>, 1, 256, 0, s, A + (long long)b0 * lda + b0, lda, bs, Yb, ldy, nrhs, mode,
+                          dstatus, tiny);
+                if (b0 > 0) {
+                    if (mode == 2)
+                        RL_LAUNCH(gemv_update_kernel<T>, std::min(gridr, ceil_div(b0, wpb)), 32 * wpb, 0, s, A + b0, lda,
+                                  b0, bs, Yb, ldy, Y, nrhs, false);
+                    else
+                        RL_LAUNCH(gemv_update_kernel<T>, ceil_div(b0, 256), 256, 0, s, A + (long long)b0 * lda, lda, b0,
+                                  bs, Yb, ldy, Y, nrhs, true);
+                }
+            }
+        }
+        return RL_OK;
+    }
+    const size_t tsm = sizeof(T) * (64 * 65 + 64 * 64);
+    RL_TRY(set_smem(trsm_diag_kernel<T>, tsm));
+    const int gr = ceil_div(nrhs, 64);
+    if (mode == 0 || mode == 1) {
+        for (int b0 = 0; b0 < n; b0 += NB) {
+            const int bs = std::min(NB, n - b0);
+            const T *D = A + (long long)b0 * lda + b0;
+            T *Yb = Y + (long long)b0 * ldy;
+            RL_LAUNCH(trsm_diag_kernel<T>, gr, 64, tsm, s, D, lda, bs, Yb, ldy, nrhs, mode, dstatus, tiny);
+            const int rest = n - b0 - bs;
+            if (rest > 0)
+                RL_TRY((gemm<T, false, false>(rest, nrhs, bs, T(-1), A + (long long)(b0 + bs) * lda + b0, lda, Yb, ldy,
+                                              T(1), Yb + (long long)bs * ldy, ldy, s)));
+        }
+    } else {
+        for (int b1 = n; b1 > 0; b1 -= NB) {
+            const int b0 = std::max(0, b1 - NB), bs = b1 - b0;
+            const T *D = A + (long long)b0 * lda + b0;
+            T *Yb = Y + (long long)b0 * ldy;
+            RL_LAUNCH(trsm_diag_kernel<T>, gr, 64, tsm, s, D, lda, bs, Yb, ldy, nrhs, mode, dstatus, tiny);
+            if (b0 > 0) {
+                if (mode == 2)
+                    RL_TRY((gemm<T, false, false>(b0, nrhs, bs, T(-1), A + b0, lda, Yb, ldy, T(1), Y, ldy, s)));
+                else
+                    RL_TRY((gemm<T, true, false>(b0, nrhs, bs, T(-1), A + (long long)b0 * lda, lda, Yb, ldy, T(1), Y,
+                                                 ldy, s)));
+            }
+        }
+    }
+    return RL_OK;
+}
+
+static __global__ void ipiv_to_perm_kernel(const int *ipiv, int n, uint64_t *perm, uint64_t *scratch) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    for (int i = 0; i < n; i++) scratch[i] = i;
+    for (int j = 0; j < n; j++) {
+        const int p = ipiv[j];
+        const uint64_t t = scratch[j];
+        scratch[j] = scratch[p];
+        scratch[p] = t;
+    }
+    for (int i = 0; i < n; i++) perm[scratch[i]] = i;  // the stored form is the inverse
+}
+
+// Solve with factors already on the device. kind 0 = LU (dperm: stored permutation),
+// 1 = Cholesky. B (n x nrhs, stride ldb) is overwritten.
+template <class T>
+rl_status factor_solve_dev(const T *F, long long lda, int n, int kind, const uint64_t *dperm, T *B, long long ldb,
+                           int nrhs, cudaStream_t s) {
+    if (n <= 0 || nrhs <= 0) return RL_OK;
+    DevBuf<int> st;
+    RL_TRY(st.alloc(1, s));
+    RL_TRY_CUDA(cudaMemsetAsync(st.p, 0, sizeof(int), s));
+    if (n <= CTA_NMAX) {
+        const size_t smem = cta_smem_bytes<T>();
+        RL_TRY(set_smem(solve_one_kernel<T>, smem));
+        RL_LAUNCH(solve_one_kernel<T>, nrhs, CTA_THREADS, smem, s, F, (int)lda, n, kind, kind ? nullptr : dperm, B, ldb,
+                  st.p, Eps<T>::value);
+        return read_status<T>(st.p, s);
+    }
+    if (kind == 1) {
+        RL_TRY(tri_solve_dev<T>(F, lda, n, B, ldb, nrhs, 1, st.p, s));
+        RL_TRY(tri_solve_dev<T>(F, lda, n, B, ldb, nrhs, 3, st.p, s));
+        return read_status<T>(st.p, s);
+    }
+    DevBuf<T> Y;
+    RL_TRY(Y.alloc((size_t)n * nrhs, s));
+    const long long tot = (long long)n * nrhs;
+    RL_LAUNCH(permute_rows_kernel<T>, (int)((tot + 255) / 256), 256, 0, s, B, ldb, Y.p, (long long)nrhs, n, nrhs,
+              dperm);
+    RL_TRY(tri_solve_dev<T>(F, lda, n, Y.p, nrhs, nrhs, 0, st.p, s));
+    RL_TRY(tri_solve_dev<T>(F, lda, n, Y.p, nrhs, nrhs, 2, st.p, s));
+    RL_TRY_CUDA(cudaMemcpy2DAsync(B, ldb * sizeof(T), Y.p, nrhs * sizeof(T), nrhs * sizeof(T), n,
+                                  cudaMemcpyDeviceToDevice, s));
+    return read_status<T>(st.p, s);
+}
+
+inline rl_status check_perm(size_t n, const uint64_t *perm) {
+    std::vector<unsigned char> seen(n, 0);
+    for (size_t i = 0; i < n; i++) {
+        if (perm[i] >= n || seen[perm[i]]) return RL_ERR_INVALID_PERMUTATION;
+        seen[perm[i]] = 1;
+    }
+    return RL_OK;
+}
+
+inline bool fits_int(size_t v) { return v <= (size_t)INT32_MAX; }
+
+}  // namespace rl

@@ -26,7 +26,9 @@ namespace rl {
 constexpr int CTA_THREADS = 256;
 constexpr int CTA_WARPS = CTA_THREADS / 32;
 constexpr int CTA_NMAX = 512;
-constexpr int CTA_LDP = CTA_NMAX + 64;  // panel column stride (slack for 64-row tiles)
+constexpr int CTA_LDP = CTA_NMAX + 72;  // panel column stride: slack for 64-row tiles; 72 = 8 mod 32
+                                        // so that a warp's 4 rows x 8 columns hit distinct banks
+                                        // pairwise, and columns stay 16-byte aligned
 
 template <class T>
 struct CtaNB;
@@ -44,15 +46,22 @@ template <class T>
 struct CtaSmem {
     static constexpr int NB = CtaNB<T>::value;
     T P[NB * CTA_LDP];     // panel, column-major: P[c * CTA_LDP + r]
-    T Bt[NB * 64];         // one 64-column slice of U12
+    T Bt[NB * 128];        // one 128-column slice of U12
     T Linv[NB * (NB + 1)]; // L11^-1 of the current LU panel
     T w[CTA_NMAX];         // factor-precision right-hand side / solution
     double x[CTA_NMAX];    // FP64 solution (refinement)
     double r[CTA_NMAX];    // FP64 residual
     int piv[CTA_NMAX];     // LAPACK-style pivots: step j swapped rows j and piv[j]
+    T cand[2][CTA_WARPS + 1][NB];  // per-warp pivot candidate rows (+ the position-j row),
+                                   // double-buffered by column parity
+    T colj[2][NB];                 // Cholesky: column j on the diagonal block's rows
+    int moved_dst[2 * NB];         // panel rows whose position changed: destination ...
+    int moved_src[2 * NB];         // ... and source (panel-relative)
+    int nmoved;
     double redd[CTA_WARPS * 2];
-    T redv[CTA_WARPS];
-    int redi[CTA_WARPS];
+    T redv[2][CTA_WARPS];
+    int redi[2][CTA_WARPS];  // position of the warp's candidate
+    int redq[2][CTA_WARPS];  // panel row of the warp's candidate
     int status;
     int item;
 };
@@ -73,6 +82,78 @@ __device__ __forceinline__ void ld4<double>(const double *p, double (&o)[4]) {
     o[0] = a.x, o[1] = a.y, o[2] = b.x, o[3] = b.y;
 }
 
+// row[0..4) -= acc[0..4) for the columns that exist (< lim); 128-bit when `vec` (row
+// 16-byte aligned) and all four exist.
+__device__ __forceinline__ void rmw4(float *row, const float (&acc)[4], int lim, bool vec) {
+    if (vec && lim >= 4) {
+        float4 v = *reinterpret_cast<float4 *>(row);
+        v.x -= acc[0], v.y -= acc[1], v.z -= acc[2], v.w -= acc[3];
+        *reinterpret_cast<float4 *>(row) = v;
+    } else {
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+            if (j < lim) row[j] -= acc[j];
+    }
+}
+__device__ __forceinline__ void rmw4(double *row, const double (&acc)[4], int lim, bool vec) {
+    if (vec && lim >= 4) {
+        double2 a = reinterpret_cast<double2 *>(row)[0], b = reinterpret_cast<double2 *>(row)[1];
+        a.x -= acc[0], a.y -= acc[1], b.x -= acc[2], b.y -= acc[3];
+        reinterpret_cast<double2 *>(row)[0] = a;
+        reinterpret_cast<double2 *>(row)[1] = b;
+    } else {
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+            if (j < lim) row[j] -= acc[j];
+    }
+}
+
+// Global 4-element row segment load / store (128-bit when `vec` and all 4 exist).
+template <class T>
+__device__ __forceinline__ void gld4(const T *row, T (&v)[4], int lim, bool vec) {
+    if (vec && lim >= 4) {
+        ld4<T>(row, v);
+    } else {
+#pragma unroll
+        for (int j = 0; j < 4; j++) v[j] = j < lim ? row[j] : T(0);
+    }
+}
+__device__ __forceinline__ void gst4(float *row, const float (&v)[4], int lim, bool vec) {
+    if (vec && lim >= 4) {
+        *reinterpret_cast<float4 *>(row) = make_float4(v[0], v[1], v[2], v[3]);
+    } else {
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+            if (j < lim) row[j] = v[j];
+    }
+}
+__device__ __forceinline__ void gst4(double *row, const double (&v)[4], int lim, bool vec) {
+    if (vec && lim >= 4) {
+        reinterpret_cast<double2 *>(row)[0] = make_double2(v[0], v[1]);
+        reinterpret_cast<double2 *>(row)[1] = make_double2(v[2], v[3]);
+    } else {
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+            if (j < lim) row[j] = v[j];
+    }
+}
+
+// Element idx of a rows x kb panel copy -> (r, c). When kb is a multiple of 8 every
+// warp instruction covers 4 rows x 8 columns: 32-byte global segments per row and
+// (with CTA_LDP = 8 mod 32) at most 2-way shared-memory bank conflicts on the
+// column-major panel. Rows are padded to a multiple of 4 (callers check r < rows).
+__device__ __forceinline__ void panel_rc(int idx, int kb, int &r, int &c) {
+    if ((kb & 7) == 0) {
+        const int lane = idx & 31, t = idx >> 5, groups = kb >> 3;
+        c = ((t % groups) << 3) + (lane & 7);
+        r = ((t / groups) << 2) + (lane >> 3);
+    } else {
+        r = idx / kb;
+        c = idx - r * kb;
+    }
+}
+__device__ __forceinline__ int panel_elems(int rows, int kb) { return ((kb & 7) == 0 ? (rows + 3) & ~3 : rows) * kb; }
+
 // (|v|, index) maximum with the smallest index winning ties.
 template <class T>
 __device__ __forceinline__ void amax_combine(T &v, int &i, T v2, int i2) {
@@ -90,6 +171,41 @@ __device__ __forceinline__ void warp_amax(T &v, int &i) {
         int i2 = __shfl_xor_sync(0xffffffffu, i, o);
         amax_combine(v, i, v2, i2);
     }
+}
+
+template <class T>
+__device__ __forceinline__ void warp_amax3(T &v, int &i, int &q) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        T v2 = __shfl_xor_sync(0xffffffffu, v, o);
+        int i2 = __shfl_xor_sync(0xffffffffu, i, o);
+        int q2 = __shfl_xor_sync(0xffffffffu, q, o);
+        if (v2 > v || (v2 == v && i2 < i)) {
+            v = v2;
+            i = i2;
+            q = q2;
+        }
+    }
+}
+
+// FP32 version on the hardware warp reductions: the largest |v| (non-negative floats
+// order like their bits; NaN and the -1 "none" sentinel map to key 0), then the smallest
+// position among the lanes holding it, then that lane's payload.
+__device__ __forceinline__ void warp_amax3(float &v, int &i, int &q) {
+    const unsigned key = (v >= 0.f) ? __float_as_uint(v) + 1u : 0u;
+    const unsigned kmax = __reduce_max_sync(0xffffffffu, key);
+    const unsigned ip = (key == kmax && key != 0u) ? (unsigned)i : 0xffffffffu;
+    const unsigned imin = __reduce_min_sync(0xffffffffu, ip);
+    if (kmax == 0u) {
+        v = -1.f;
+        i = INT_MAX;
+        q = -1;
+        return;
+    }
+    const int src = __ffs(__ballot_sync(0xffffffffu, ip == imin)) - 1;
+    v = __shfl_sync(0xffffffffu, v, src);
+    q = __shfl_sync(0xffffffffu, q, src);
+    i = (int)imin;
 }
 
 template <class T>
@@ -119,6 +235,104 @@ __device__ double block_max(double v, CtaSmem<T> &S) {
     return m;
 }
 
+// Panel copies between global memory (row-major, row stride lda, from A[k0][k0]) and
+// the column-major shared panel, K elements per thread per round so that K independent
+// loads are in flight. LOWER_ONLY copies the elements on or below the diagonal only.
+template <class T, bool LOWER_ONLY>
+__device__ __forceinline__ void panel_load(const T *__restrict__ A, int lda, int k0, int mrows, int kb, CtaSmem<T> &S) {
+    constexpr int K = 8;
+    const int pe = panel_elems(mrows, kb);
+    for (int base = threadIdx.x; base < pe; base += CTA_THREADS * K) {
+        T v[K];
+        int off[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const int idx = base + k * CTA_THREADS;
+            int r, c;
+            panel_rc(idx, kb, r, c);
+            const bool ok = idx < pe && r < mrows && (!LOWER_ONLY || r >= c);
+            off[k] = ok ? c * CTA_LDP + r : -1;
+            v[k] = ok ? A[(long long)(k0 + r) * lda + k0 + c] : T(0);
+        }
+#pragma unroll
+        for (int k = 0; k < K; k++)
+            if (off[k] >= 0) S.P[off[k]] = v[k];
+    }
+}
+
+template <class T, bool LOWER_ONLY>
+__device__ __forceinline__ void panel_store(T *__restrict__ A, int lda, int k0, int mrows, int kb, const CtaSmem<T> &S) {
+    const int pe = panel_elems(mrows, kb);
+    for (int idx = threadIdx.x; idx < pe; idx += CTA_THREADS) {
+        int r, c;
+        panel_rc(idx, kb, r, c);
+        if (r < mrows && (!LOWER_ONLY || r >= c)) A[(long long)(k0 + r) * lda + k0 + c] = S.P[c * CTA_LDP + r];
+    }
+}
+
+
+// One trailing-update tile: C -= L * U over NB, with L read from the shared panel at
+// panel rows rb + h*64 + {0..3} (h < H) and U read from shared memory at bs[p * ldb +
+// cb + h*64 + {0..3}]; C is global at A[(k0 + row) * lda + k0 + ccol], with at most
+// `lim(row, col)` existing columns from col on. Every thread holds (4H) x (4H) outputs:
+// H = 2 (128 x 128 tiles) for FP32, H = 1 (64 x 64) for FP64 (register budget).
+template <class T>
+struct TileCfg {
+    static constexpr int H = sizeof(T) == 4 ? 2 : 1;
+    static constexpr int TS = 64 * H;
+};
+
+template <class T, int NB, class Lim>
+__device__ __forceinline__ void update_tile(T *__restrict__ A, int lda, int k0, int mrows, int row0, int col0,
+                                           const T *__restrict__ P, const T *__restrict__ bs, int ldb, int bcol0,
+                                           bool vec, Lim lim) {
+    constexpr int H = TileCfg<T>::H, R = 4 * H;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    T cv[R][R];
+#pragma unroll
+    for (int i = 0; i < R; i++) {
+        const int r = row0 + (i >> 2) * 64 + ty * 4 + (i & 3);
+#pragma unroll
+        for (int h = 0; h < H; h++) {
+            const int c = col0 + h * 64 + tx * 4;
+            T t4[4];
+            if (r < mrows)
+                gld4<T>(A + (long long)(k0 + r) * lda + k0 + c, t4, lim(r, c), vec);
+            else
+#pragma unroll
+                for (int j = 0; j < 4; j++) t4[j] = T(0);
+#pragma unroll
+            for (int j = 0; j < 4; j++) cv[i][h * 4 + j] = t4[j];
+        }
+    }
+#pragma unroll 4
+    for (int p = 0; p < NB; p++) {
+        T a[R], b[R];
+#pragma unroll
+        for (int h = 0; h < H; h++) {
+            ld4<T>(&P[p * CTA_LDP + row0 + h * 64 + ty * 4], *reinterpret_cast<T(*)[4]>(&a[h * 4]));
+            ld4<T>(&bs[p * ldb + bcol0 + h * 64 + tx * 4], *reinterpret_cast<T(*)[4]>(&b[h * 4]));
+        }
+#pragma unroll
+        for (int i = 0; i < R; i++)
+#pragma unroll
+            for (int j = 0; j < R; j++) cv[i][j] = fma(-a[i], b[j], cv[i][j]);
+    }
+#pragma unroll
+    for (int i = 0; i < R; i++) {
+        const int r = row0 + (i >> 2) * 64 + ty * 4 + (i & 3);
+        if (r >= mrows) continue;
+#pragma unroll
+        for (int h = 0; h < H; h++) {
+            const int c = col0 + h * 64 + tx * 4;
+            T t4[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) t4[j] = cv[i][h * 4 + j];
+            gst4(A + (long long)(k0 + r) * lda + k0 + c, t4, lim(r, c), vec);
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------- LU --
 // Factors the n x n matrix A (row stride lda) in place; S.piv receives the pivots.
 // A pivot with |p| < tiny returns RL_ERR_DIV_BY_ZERO (tiny = epsilon reproduces the
@@ -126,76 +340,186 @@ __device__ double block_max(double v, CtaSmem<T> &S) {
 template <class T>
 __device__ int cta_lu_factor(T *__restrict__ A, int lda, int n, CtaSmem<T> &S, T tiny) {
     constexpr int NB = CtaNB<T>::value;
+    constexpr int RPT = CTA_NMAX / CTA_THREADS;  // panel rows per thread
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // 128-bit trailing-update accesses when every row start is 16-byte aligned
+    const bool vec = (lda % 4) == 0 && (reinterpret_cast<uintptr_t>(A) % 16) == 0;
     for (int k0 = 0; k0 < n; k0 += NB) {
         const int kb = min(NB, n - k0), mrows = n - k0;
-        for (int idx = tid; idx < mrows * kb; idx += CTA_THREADS) {
-            const int r = idx / kb, c = idx - r * kb;
-            S.P[c * CTA_LDP + r] = A[(long long)(k0 + r) * lda + k0 + c];
+        // The panel lives in registers: thread t holds panel rows t and t + 256 (row q
+        // of the panel is A[k0 + q][k0 .. k0 + kb)). Rows never move; pos[k] is the
+        // row's current position (swaps exchange positions) and used[k] marks a row that
+        // has become a pivot row.
+        T row[RPT][NB];
+        int pos[RPT];
+        bool used[RPT];
+#pragma unroll
+        for (int k = 0; k < RPT; k++) {
+            const int q = tid + k * CTA_THREADS;
+            pos[k] = q;
+            used[k] = q >= mrows;
+            const T *src = A + (long long)(k0 + q) * lda + k0;
+#pragma unroll
+            for (int c = 0; c < NB; c++) row[k][c] = (q < mrows && c < kb) ? src[c] : T(0);
         }
-        __syncthreads();
-        for (int j = 0; j < kb; j++) {
-            T *col = S.P + j * CTA_LDP;
+        if (tid == 0) S.nmoved = 0;
+        // One barrier per column. Step j: the warps' argmax candidates for column j (and
+        // their rows) were published in the previous step; every thread combines them,
+        // then updates its own active rows with the pivot row and forms its candidate for
+        // column j + 1, which its warp publishes for the next step.
+        auto publish = [&](int j, int par) {
             T bv = T(-1);
-            int bi = INT_MAX;
-            for (int r = j + tid; r < mrows; r += CTA_THREADS) {
-                const T v = absT(col[r]);
-                if (v > bv) {
-                    bv = v;
-                    bi = r;
+            int bi = INT_MAX, bq = -1, bk = -1;
+#pragma unroll
+            for (int k = 0; k < RPT; k++) {
+                T v = T(0);
+#pragma unroll
+                for (int c = 0; c < NB; c++)
+                    if (c == j) v = row[k][c];
+                const T av = absT(v);
+                if (!used[k] && (av > bv || (av == bv && pos[k] < bi))) {
+                    bv = av;
+                    bi = pos[k];
+                    bq = tid + k * CTA_THREADS;
+                    bk = k;
+                }
+                if (pos[k] == j && tid + k * CTA_THREADS < mrows) {  // the row at position j (NaN fallback)
+#pragma unroll
+                    for (int c = 0; c < NB; c++) S.cand[par][CTA_WARPS][c] = row[k][c];
                 }
             }
-            warp_amax(bv, bi);
-            if (lane == 0) {
-                S.redv[warp] = bv;
-                S.redi[warp] = bi;
-            }
-            __syncthreads();
-            bv = S.redv[0];
-            bi = S.redi[0];
+            T wv = bv;
+            int wi = bi, wq = bq;
+            warp_amax3(wv, wi, wq);
+            if (wq >= 0 && wq == bq && bk >= 0) {  // this lane holds the warp's winner
 #pragma unroll
-            for (int w = 1; w < CTA_WARPS; w++) amax_combine(bv, bi, S.redv[w], S.redi[w]);
-            if (bi == INT_MAX) {  // column of NaNs: keep the diagonal, as the reference does
+                for (int k = 0; k < RPT; k++)
+                    if (k == bk)
+#pragma unroll
+                        for (int c = 0; c < NB; c++) S.cand[par][warp][c] = row[k][c];
+            }
+            if (lane == 0) {
+                S.redv[par][warp] = wv;
+                S.redi[par][warp] = wi;
+                S.redq[par][warp] = wq;
+            }
+        };
+        publish(0, 0);
+        // Fully unrolled over the panel's columns: j is a compile-time constant in every
+        // copy, so the column selects and the c > j predicates cost nothing.
+#pragma unroll
+        for (int j = 0; j < NB; j++) {
+            if (j >= kb) break;
+            const int par = j & 1;
+            __syncthreads();
+            T bv = S.redv[par][0];
+            int bi = S.redi[par][0], bq = S.redq[par][0], bw = 0;
+#pragma unroll
+            for (int w = 1; w < CTA_WARPS; w++) {
+                const T v2 = S.redv[par][w];
+                const int i2 = S.redi[par][w];
+                if (v2 > bv || (v2 == bv && i2 < bi)) {
+                    bv = v2;
+                    bi = i2;
+                    bq = S.redq[par][w];
+                    bw = w;
+                }
+            }
+            if (bi == INT_MAX) {  // no comparable candidate (NaNs): keep the diagonal, as the reference does
                 bi = j;
-                bv = absT(col[j]);
+                bq = -1;
+                bw = CTA_WARPS;
+                T d = S.cand[par][CTA_WARPS][0];
+#pragma unroll
+                for (int c = 0; c < NB; c++)
+                    if (c == j) d = S.cand[par][CTA_WARPS][c];
+                bv = absT(d);
             }
             if (bv < tiny) {
                 __syncthreads();
                 return RL_ERR_DIV_BY_ZERO;
             }
-            if (bi != j && tid < kb) {
-                T *cc = S.P + tid * CTA_LDP;
-                const T t = cc[j];
-                cc[j] = cc[bi];
-                cc[bi] = t;
-            }
             if (tid == 0) S.piv[k0 + j] = k0 + bi;
-            __syncthreads();
-            const T p = col[j];
-            for (int r = j + 1 + tid; r < mrows; r += CTA_THREADS) {
-                const T l = col[r] / p;
-                col[r] = l;
-                for (int c = j + 1; c < kb; c++) S.P[c * CTA_LDP + r] = fma(-l, S.P[c * CTA_LDP + j], S.P[c * CTA_LDP + r]);
-            }
-            __syncthreads();
-        }
-        for (int idx = tid; idx < mrows * kb; idx += CTA_THREADS) {
-            const int r = idx / kb, c = idx - r * kb;
-            A[(long long)(k0 + r) * lda + k0 + c] = S.P[c * CTA_LDP + r];
-        }
-        // Row swaps of this panel on all other columns: each thread owns whole columns
-        // and replays the panel's swaps in order.
-        for (int c = tid; c < n - kb; c += CTA_THREADS) {
-            const int gc = c < k0 ? c : c + kb;
-            for (int j = 0; j < kb; j++) {
-                const int pr = S.piv[k0 + j];
-                if (pr != k0 + j) {
-                    T *a0 = A + (long long)(k0 + j) * lda + gc;
-                    T *a1 = A + (long long)pr * lda + gc;
-                    const T t = *a0;
-                    *a0 = *a1;
-                    *a1 = t;
+            T prow[NB];
+#pragma unroll
+            for (int c = 0; c < NB; c++) prow[c] = S.cand[par][bw][c];
+            T p = prow[0];
+#pragma unroll
+            for (int c = 0; c < NB; c++)
+                if (c == j) p = prow[c];
+            const T inv_p = T(1) / p;  // one division per column; multipliers l = a_rj * (1/p)
+#pragma unroll
+            for (int k = 0; k < RPT; k++) {
+                const int q = tid + k * CTA_THREADS;
+                const bool is_piv = (bq >= 0) ? (q == bq) : (pos[k] == j && q < mrows);
+                if (is_piv) {
+                    used[k] = true;
+                    pos[k] = j;
+                } else if (pos[k] == j) {
+                    pos[k] = bi;  // the row that held position j takes the pivot's old position
                 }
+                if (used[k]) continue;
+                T lj = row[k][0];
+#pragma unroll
+                for (int c = 0; c < NB; c++)
+                    if (c == j) lj = row[k][c];
+                const T l = lj * inv_p;
+#pragma unroll
+                for (int c = 0; c < NB; c++) {
+                    if (c > j) row[k][c] = fma(-l, prow[c], row[k][c]);
+                    if (c == j) row[k][c] = l;
+                }
+            }
+            if (j + 1 < kb) publish(j + 1, par ^ 1);
+        }
+        __syncthreads();
+        // Rows to their final positions: shared panel (column-major, position order, for
+        // the trailing update), global A, and the list of rows whose position changed.
+#pragma unroll
+        for (int k = 0; k < RPT; k++) {
+            const int q = tid + k * CTA_THREADS;
+            if (q >= mrows) continue;
+            T *dst = A + (long long)(k0 + pos[k]) * lda + k0;
+#pragma unroll
+            for (int c = 0; c < NB; c++) {
+                if (c < kb) {
+                    S.P[c * CTA_LDP + pos[k]] = row[k][c];
+                    dst[c] = row[k][c];
+                }
+            }
+            if (pos[k] != q) {
+                const int m = atomicAdd(&S.nmoved, 1);
+                S.moved_dst[m] = pos[k];
+                S.moved_src[m] = q;
+            }
+        }
+        __syncthreads();
+        // The panel's row permutation on every other column, 64 columns at a time: the
+        // (at most 2 NB) moved rows' sources are staged in shared memory (all loads in
+        // flight), then written to their destinations.
+        {
+            const int nmv = S.nmoved;
+            T *stage = S.Bt;  // NB * 64 >= 2 NB rows x 32 columns
+            constexpr int CW = 32;
+            for (int c0 = 0; c0 < n - kb && nmv > 0; c0 += CW) {
+                constexpr int K = (2 * NB * CW) / CTA_THREADS;
+                T v[K];
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    const int e = tid + k * CTA_THREADS, m = e / CW, cc = e % CW, c = c0 + cc;
+                    const int gc = c < k0 ? c : c + kb;
+                    v[k] = (m < nmv && c < n - kb) ? A[(long long)(k0 + S.moved_src[m]) * lda + gc] : T(0);
+                }
+#pragma unroll
+                for (int k = 0; k < K; k++) stage[tid + k * CTA_THREADS] = v[k];
+                __syncthreads();
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    const int e = tid + k * CTA_THREADS, m = e / CW, cc = e % CW, c = c0 + cc;
+                    const int gc = c < k0 ? c : c + kb;
+                    if (m < nmv && c < n - kb) A[(long long)(k0 + S.moved_dst[m]) * lda + gc] = stage[e];
+                }
+                __syncthreads();
             }
         }
         __syncthreads();
@@ -212,62 +536,47 @@ __device__ int cta_lu_factor(T *__restrict__ A, int lda, int n, CtaSmem<T> &S, T
             if (lane < NB) S.Linv[lane * (NB + 1) + j] = x;
         }
         __syncthreads();
-        // Per 64-column slice: U12 = L11^-1 A12 as a small shared-memory GEMM (written
-        // back to A), then A22 -= L21 * U12 over all row tiles, 4 x 4 outputs per thread.
+        // Per 128-column slice: U12 = L11^-1 A12 as a small shared-memory GEMM (written
+        // back to A), then A22 -= L21 * U12 tile by tile (update_tile).
         const int m2 = mrows - kb;
-        const int tx = tid & 15, ty = tid >> 4;
-        constexpr int RPT = NB / 4;  // U12 rows per thread in the slice solve
-        for (int tj = 0; tj < n2; tj += 64) {
-            for (int idx = tid; idx < NB * 64; idx += CTA_THREADS) {
-                const int p = idx >> 6, cc = idx & 63;
-                S.Bt[idx] = (tj + cc < n2) ? A[(long long)(k0 + p) * lda + k0 + kb + tj + cc] : T(0);
+        constexpr int RPS = NB / 2;  // U12 rows per thread in the slice solve
+        for (int tj = 0; tj < n2; tj += 128) {
+            {
+                constexpr int K = NB * 128 / CTA_THREADS;
+                T v[K];
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    const int idx = tid + k * CTA_THREADS, pp = idx >> 7, cc = idx & 127;
+                    v[k] = (tj + cc < n2) ? A[(long long)(k0 + pp) * lda + k0 + kb + tj + cc] : T(0);
+                }
+#pragma unroll
+                for (int k = 0; k < K; k++) S.Bt[tid + k * CTA_THREADS] = v[k];
             }
             __syncthreads();
             {
-                const int cc = tid & 63, rg = (tid >> 6) * RPT;
-                T u[RPT];
+                const int cc = tid & 127, rg = (tid >> 7) * RPS;
+                T u[RPS];
 #pragma unroll
-                for (int i = 0; i < RPT; i++) u[i] = T(0);
+                for (int i = 0; i < RPS; i++) u[i] = T(0);
 #pragma unroll
                 for (int k = 0; k < NB; k++) {
-                    const T bk = S.Bt[k * 64 + cc];
+                    const T bk = S.Bt[k * 128 + cc];
 #pragma unroll
-                    for (int i = 0; i < RPT; i++) u[i] = fma(S.Linv[(rg + i) * (NB + 1) + k], bk, u[i]);
+                    for (int i = 0; i < RPS; i++) u[i] = fma(S.Linv[(rg + i) * (NB + 1) + k], bk, u[i]);
                 }
                 __syncthreads();
 #pragma unroll
-                for (int i = 0; i < RPT; i++) {
-                    S.Bt[(rg + i) * 64 + cc] = u[i];
+                for (int i = 0; i < RPS; i++) {
+                    S.Bt[(rg + i) * 128 + cc] = u[i];
                     if (tj + cc < n2) A[(long long)(k0 + rg + i) * lda + k0 + kb + tj + cc] = u[i];
                 }
             }
             __syncthreads();
-            for (int ti = 0; ti < m2; ti += 64) {
-                T acc[4][4];
-#pragma unroll
-                for (int i = 0; i < 4; i++)
-#pragma unroll
-                    for (int j = 0; j < 4; j++) acc[i][j] = T(0);
-                const int rb = kb + ti + ty * 4;
-#pragma unroll 8
-                for (int p = 0; p < NB; p++) {
-                    T a[4], b[4];
-                    ld4<T>(&S.P[p * CTA_LDP + rb], a);
-                    ld4<T>(&S.Bt[p * 64 + tx * 4], b);
-#pragma unroll
-                    for (int i = 0; i < 4; i++)
-#pragma unroll
-                        for (int j = 0; j < 4; j++) acc[i][j] = fma(a[i], b[j], acc[i][j]);
-                }
-#pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    if (rb + i >= mrows) break;
-                    T *row = A + (long long)(k0 + rb + i) * lda + k0 + kb + tj + tx * 4;
-#pragma unroll
-                    for (int j = 0; j < 4; j++)
-                        if (tj + tx * 4 + j < n2) row[j] -= acc[i][j];
-                }
-            }
+            constexpr int TS = TileCfg<T>::TS;
+            for (int ti = 0; ti < m2; ti += TS)
+                for (int tc = 0; tc < 128 && tj + tc < n2; tc += TS)
+                    update_tile<T, NB>(A, lda, k0, mrows, kb + ti, kb + tj + tc, S.P, S.Bt, 128, tc, vec,
+                                       [&](int, int c) { return kb + n2 - c; });
             __syncthreads();
         }
     }
@@ -281,74 +590,89 @@ __device__ int cta_lu_factor(T *__restrict__ A, int lda, int n, CtaSmem<T> &S, T
 template <class T>
 __device__ int cta_chol_factor(T *__restrict__ A, int lda, int n, CtaSmem<T> &S, T tiny) {
     constexpr int NB = CtaNB<T>::value;
+    constexpr int RPT = CTA_NMAX / CTA_THREADS;  // panel rows per thread
     const int tid = threadIdx.x;
+    const bool vec = (lda % 4) == 0 && (reinterpret_cast<uintptr_t>(A) % 16) == 0;
     for (int k0 = 0; k0 < n; k0 += NB) {
         const int kb = min(NB, n - k0), mrows = n - k0;
-        for (int idx = tid; idx < mrows * kb; idx += CTA_THREADS) {
-            const int r = idx / kb, c = idx - r * kb;
-            if (r >= c) S.P[c * CTA_LDP + r] = A[(long long)(k0 + r) * lda + k0 + c];
+        // The panel lives in registers (thread t holds rows t and t + 256, lower part
+        // only). One barrier per column: the diagonal block's column j is published to
+        // shared memory by its rows' owners at the end of step j - 1.
+        T row[RPT][NB];
+#pragma unroll
+        for (int k = 0; k < RPT; k++) {
+            const int q = tid + k * CTA_THREADS;
+            const T *src = A + (long long)(k0 + q) * lda + k0;
+#pragma unroll
+            for (int c = 0; c < NB; c++) row[k][c] = (q < mrows && c < kb && c <= q) ? src[c] : T(0);
         }
-        __syncthreads();
-        for (int j = 0; j < kb; j++) {
-            T *col = S.P + j * CTA_LDP;
-            const T d = col[j];
+        if (tid < kb) S.colj[0][tid] = row[0][0];
+        // Fully unrolled over the panel's columns (j is a compile-time constant per copy).
+#pragma unroll
+        for (int j = 0; j < NB; j++) {
+            if (j >= kb) break;
+            const int par = j & 1;
+            __syncthreads();
+            const T d = S.colj[par][j];
             if (absT(d) < tiny || d < T(0)) {
                 __syncthreads();
                 return RL_ERR_DECOMP_FAILURE;
             }
             const T s = sqrt(d);
-            __syncthreads();
-            for (int r = j + tid; r < mrows; r += CTA_THREADS) col[r] = col[r] / s;
-            __syncthreads();
-            for (int r = j + 1 + tid; r < mrows; r += CTA_THREADS) {
-                const T l = col[r];
-                const int cmax = min(kb - 1, r);
-                for (int c = j + 1; c <= cmax; c++) S.P[c * CTA_LDP + r] = fma(-l, col[c], S.P[c * CTA_LDP + r]);
+            const T inv = T(1) / s;  // update factors; the stored entries keep the division
+            T lc[NB];
+#pragma unroll
+            for (int c = 0; c < NB; c++) lc[c] = S.colj[par][c] * inv;
+#pragma unroll
+            for (int k = 0; k < RPT; k++) {
+                const int q = tid + k * CTA_THREADS;
+                if (q < j || q >= mrows) continue;
+                T cr = row[k][0];
+#pragma unroll
+                for (int c = 0; c < NB; c++)
+                    if (c == j) cr = row[k][c];
+                const T l = cr / s, li = cr * inv;
+#pragma unroll
+                for (int c = 0; c < NB; c++) {
+                    if (c > j && c <= q && c < kb) row[k][c] = fma(-li, lc[c], row[k][c]);
+                    if (c == j) row[k][c] = l;
+                }
             }
-            __syncthreads();
+            if (j + 1 < kb && tid < kb) {  // rows tid < kb are row[0] of threads 0..kb-1
+                T v = row[0][0];
+#pragma unroll
+                for (int c = 0; c < NB; c++)
+                    if (c == j + 1) v = row[0][c];
+                S.colj[par ^ 1][tid] = v;
+            }
         }
-        for (int idx = tid; idx < mrows * kb; idx += CTA_THREADS) {
-            const int r = idx / kb, c = idx - r * kb;
-            if (r >= c) A[(long long)(k0 + r) * lda + k0 + c] = S.P[c * CTA_LDP + r];
+        // Write the factored panel: shared (column-major, for the SYRK) and global (the
+        // lower part only; the strict upper triangle is never written).
+#pragma unroll
+        for (int k = 0; k < RPT; k++) {
+            const int q = tid + k * CTA_THREADS;
+            if (q >= mrows) continue;
+            T *dst = A + (long long)(k0 + q) * lda + k0;
+#pragma unroll
+            for (int c = 0; c < NB; c++) {
+                if (c < kb && c <= q) {
+                    S.P[c * CTA_LDP + q] = row[k][c];
+                    dst[c] = row[k][c];
+                }
+            }
         }
+        __syncthreads();
         const int m2 = mrows - kb;
         if (m2 <= 0) {
             __syncthreads();
             continue;
         }
         // A22 -= L21 L21^T on the lower triangle; both operands come from the panel.
-        const int tx = tid & 15, ty = tid >> 4;
-        for (int ti = 0; ti < m2; ti += 64) {
-            for (int tj = 0; tj <= ti; tj += 64) {
-                T acc[4][4];
-#pragma unroll
-                for (int i = 0; i < 4; i++)
-#pragma unroll
-                    for (int j = 0; j < 4; j++) acc[i][j] = T(0);
-                const int rb = kb + ti + ty * 4, cb = kb + tj + tx * 4;
-#pragma unroll 8
-                for (int p = 0; p < NB; p++) {
-                    T a[4], b[4];
-                    ld4<T>(&S.P[p * CTA_LDP + rb], a);
-                    ld4<T>(&S.P[p * CTA_LDP + cb], b);
-#pragma unroll
-                    for (int i = 0; i < 4; i++)
-#pragma unroll
-                        for (int j = 0; j < 4; j++) acc[i][j] = fma(a[i], b[j], acc[i][j]);
-                }
-#pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    const int r = rb + i;
-                    if (r >= mrows) break;
-                    T *row = A + (long long)(k0 + r) * lda + k0;
-#pragma unroll
-                    for (int j = 0; j < 4; j++) {
-                        const int c = cb + j;
-                        if (c <= r && c < mrows) row[c] -= acc[i][j];
-                    }
-                }
-            }
-        }
+        constexpr int TS = TileCfg<T>::TS;
+        for (int ti = 0; ti < m2; ti += TS)
+            for (int tj = 0; tj <= ti; tj += TS)
+                update_tile<T, NB>(A, lda, k0, mrows, kb + ti, kb + tj, S.P, S.P, CTA_LDP, kb + tj, vec,
+                                   [&](int r, int c) { return min(mrows, r + 1) - c; });
         __syncthreads();
     }
     return RL_OK;

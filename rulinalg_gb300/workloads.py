@@ -75,3 +75,36 @@ def mixed_batch(count_spd: int, count_lu: int, seed: int = 0, lo: int = 8, hi: i
     elif dtype == np.float32:
         a, b = a.astype(np.float32), b.astype(np.float32)
     return n, kind, a, b
+
+
+def haar_orthogonal(n: int, rng):
+    """A Haar-distributed orthogonal matrix: QR of a Gaussian matrix with the signs of R's
+    diagonal folded into Q (Mezzadri 2007)."""
+    q, r = np.linalg.qr(rng.standard_normal((n, n)))
+    return q * np.sign(np.diag(r))
+
+
+def conditioned_system(n: int, kappa: float, nrhs: int = 1, seed: int = 0, device=None):
+    """A = U diag(sigma) V^T with U, V Haar-random orthogonal and sigma geometric from 1
+    down to 1/kappa; B with nrhs N(0,1) columns. With a torch CUDA `device` the orthogonal
+    factors and the product are formed there in FP64 (the n = 16384 case would take
+    minutes on the host) and torch tensors are returned."""
+    sigma = kappa ** (-np.arange(n) / max(n - 1, 1))
+    if device is None:
+        rng = np.random.default_rng(seed)
+        u = haar_orthogonal(n, rng)
+        v = haar_orthogonal(n, rng)
+        a = (u * sigma) @ v.T
+        b = rng.standard_normal((n, nrhs))
+        return np.ascontiguousarray(a), np.ascontiguousarray(b)
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+
+    def haar():
+        q, r = torch.linalg.qr(torch.randn(n, n, dtype=torch.float64, device=device, generator=g))
+        return q * torch.sign(torch.diagonal(r))
+    u, v = haar(), haar()
+    a = (u * torch.from_numpy(sigma).to(device)) @ v.T
+    b = torch.randn(n, nrhs, dtype=torch.float64, device=device, generator=g)
+    return a.contiguous(), b.contiguous()

@@ -1,0 +1,72 @@
+"""Mixed-precision single-system solves (FP32 factor + FP64 refinement / GMRES-IR /
+FP64 refactor) on A = U diag(sigma) V^T systems with kappa in {1e2, 1e6, 1e10}: every
+solution f64-accurate (normwise backward error <= n 2^-53 10) and close to the FP64
+oracle's solution within kappa-scaled forward error."""
+import numpy as np
+import pytest
+
+import oracle as O
+from comparators import backward_error
+
+pytestmark = pytest.mark.gpu
+U64 = 2.0 ** -53
+
+
+@pytest.mark.parametrize("kappa", [1e2, 1e6, 1e10])
+@pytest.mark.parametrize("n,nrhs", [(700, 1), (1024, 3)])
+def test_mixed_lu_conditioned(gpu, kappa, n, nrhs):
+    from rulinalg_gb300.workloads import conditioned_system
+    a, b = conditioned_system(n, kappa, nrhs, seed=int(np.log10(kappa)) + n)
+    x, info = gpu.solve_mixed(a, b, "lu")
+    lu, perm, st = O.lu_decompose(a)
+    assert st == O.OK
+    for c in range(nrhs):
+        be = backward_error(a, x[:, c], b[:, c])
+        assert be <= n * U64 * 10, (c, be, info)
+        xo, _ = O.lu_solve(lu, perm, b[:, c])
+        fe = np.max(np.abs(x[:, c] - xo)) / np.max(np.abs(xo))
+        assert fe <= max(kappa * n * U64 * 10, 1e-13), (c, fe, info)
+    assert info["berr"] <= n * U64 * 10
+    if kappa == 1e2:
+        assert info["path"] == "refinement" and 1 <= info["iters"] <= 4, info
+    print(f"n={n} kappa={kappa:.0e} nrhs={nrhs}: {info}")
+
+
+def test_mixed_cholesky_and_many_rhs(gpu):
+    rng = np.random.default_rng(5)
+    n = 600
+    g = rng.standard_normal((n, n))
+    a = g @ g.T + n * np.eye(n)
+    b = rng.standard_normal((n, 12))  # more than 4 columns: the GEMM residual path
+    x, info = gpu.solve_mixed(a, b, "cholesky")
+    for c in range(12):
+        assert backward_error(a, x[:, c], b[:, c]) <= n * U64 * 10
+    assert info["path"] == "refinement"
+
+
+def test_mixed_singular_reports_div_by_zero(gpu):
+    a = np.ones((600, 600))
+    with pytest.raises(gpu.RulinalgError) as e:
+        gpu.solve_mixed(a, np.ones(600), "lu")
+    assert e.value.kind == "DivByZero"
+
+
+def test_fp64_dev_path(gpu):
+    import torch
+    from rulinalg_gb300._lib import SolveInfo
+    import ctypes as C
+    rng = np.random.default_rng(6)
+    n = 900
+    a = rng.uniform(-1, 1, (n, n)) + np.eye(n) * 3
+    b = rng.standard_normal((n, 2))
+    dev = torch.device("cuda:0")
+    ta, tb = torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev)
+    tx = torch.zeros_like(tb)
+    info = SolveInfo()
+    st = gpu.lib.rl_dsolve_fp64_dev(n, 2, 0, ta.data_ptr(), n, tb.data_ptr(), 2, tx.data_ptr(), 2, C.byref(info),
+                                    torch.cuda.current_stream().cuda_stream)
+    assert st == 0
+    x = tx.cpu().numpy()
+    for c in range(2):
+        assert backward_error(a, x[:, c], b[:, c]) <= n * U64 * 10
+    assert info.path == 2 and info.berr <= n * U64 * 10
