@@ -90,6 +90,7 @@ __device__ void batch_solve_one(const BatchDesc &d, int sys, const TI *__restric
 
     const TF tiny = MIXED ? TF(FLT_MIN) : Eps<TF>::value;
     int st = kind ? cta_chol_factor<TF>(W, ldw, n, S, tiny) : cta_lu_factor<TF>(W, ldw, n, S, tiny);
+    if (st == RL_OK && !kind) cta_build_rowperm(n, S);
     if (st == RL_OK) {
         for (int i = tid; i < n; i += CTA_THREADS) S.w[i] = (TF)bi[i];
         __syncthreads();

@@ -52,6 +52,7 @@ struct CtaSmem {
     double x[CTA_NMAX];    // FP64 solution (refinement)
     double r[CTA_NMAX];    // FP64 residual
     int piv[CTA_NMAX];     // LAPACK-style pivots: step j swapped rows j and piv[j]
+    int rowperm[CTA_NMAX]; // the same as a position -> original row map (solves)
     T cand[2][CTA_WARPS + 1][NB];  // per-warp pivot candidate rows (+ the position-j row),
                                    // double-buffered by column parity
     T colj[2][NB];                 // Cholesky: column j on the diagonal block's rows
@@ -274,11 +275,12 @@ __device__ __forceinline__ void panel_store(T *__restrict__ A, int lda, int k0, 
 // One trailing-update tile: C -= L * U over NB, with L read from the shared panel at
 // panel rows rb + h*64 + {0..3} (h < H) and U read from shared memory at bs[p * ldb +
 // cb + h*64 + {0..3}]; C is global at A[(k0 + row) * lda + k0 + ccol], with at most
-// `lim(row, col)` existing columns from col on. Every thread holds (4H) x (4H) outputs:
-// H = 2 (128 x 128 tiles) for FP32, H = 1 (64 x 64) for FP64 (register budget).
+// `lim(row, col)` existing columns from col on. Every thread holds (4H) x (4H) outputs
+// (H = 1: 64 x 64 tiles; 8 x 8 per thread spilled under the two-CTAs-per-SM register
+// cap and padded the small trailing blocks, and measured slower).
 template <class T>
 struct TileCfg {
-    static constexpr int H = sizeof(T) == 4 ? 2 : 1;
+    static constexpr int H = 1;  // 4 x 4 per thread measured faster than 8 x 8 here
     static constexpr int TS = 64 * H;
 };
 
@@ -463,7 +465,8 @@ __device__ int cta_lu_factor(T *__restrict__ A, int lda, int n, CtaSmem<T> &S, T
 #pragma unroll
                 for (int c = 0; c < NB; c++)
                     if (c == j) lj = row[k][c];
-                const T l = lj * inv_p;
+                // FP64 keeps gaussian_elimination's division (lu.rs:609); FP32 multiplies by 1/p
+                const T l = sizeof(T) == 8 ? lj / p : lj * inv_p;
 #pragma unroll
                 for (int c = 0; c < NB; c++) {
                     if (c > j) row[k][c] = fma(-l, prow[c], row[k][c]);
@@ -679,9 +682,29 @@ __device__ int cta_chol_factor(T *__restrict__ A, int lda, int n, CtaSmem<T> &S,
 }
 
 // ------------------------------------------------------------------------- solves --
-// In-place solves on the shared vector S.w (already permuted for LU). Triangles are read
-// from global memory, 32 x 32 diagonal blocks by warp 0 with shuffles, the rest as
-// warp-per-row (or thread-per-column) GEMV updates.
+// In-place solves on the shared vector S.w. Triangles are read from global memory (the
+// factor lives in L2): each 32 x 32 diagonal block by warp 0, every lane holding its
+// block row in registers (loaded up front, all loads in flight) and the solution moving
+// by shuffles; the off-block updates with a thread per row (or per column for L^T), its
+// 32 loads issued together.
+
+// w[i] -= sum_{j < bs} M[i][j] * w[b0 + j] for the rows i in [lo, hi) of M (M points at
+// column b0 of row 0; row stride lda).
+template <class T>
+__device__ __forceinline__ void cta_block_update(const T *__restrict__ M, int lda, int lo, int hi, int b0, int bs,
+                                                 CtaSmem<T> &S) {
+    for (int i = lo + threadIdx.x; i < hi; i += CTA_THREADS) {
+        const T *row = M + (long long)i * lda;
+        T v[32];
+#pragma unroll
+        for (int j = 0; j < 32; j++) v[j] = j < bs ? row[j] : T(0);
+        T s = T(0);
+#pragma unroll
+        for (int j = 0; j < 32; j++)
+            if (j < bs) s = fma(v[j], S.w[b0 + j], s);
+        S.w[i] -= s;
+    }
+}
 
 // Unit lower triangular solve L y = w (L strictly below the diagonal of A).
 template <class T>
@@ -690,20 +713,20 @@ __device__ void cta_unit_lower_solve(const T *__restrict__ A, int lda, int n, Ct
     for (int b0 = 0; b0 < n; b0 += 32) {
         const int bs = min(32, n - b0);
         if (warp == 0) {
-            T wv = lane < bs ? S.w[b0 + lane] : T(0);
+            T lr[32];
             const T *lrow = A + (long long)(b0 + lane) * lda + b0;
-            for (int jj = 0; jj < bs - 1; jj++) {
+#pragma unroll
+            for (int jj = 0; jj < 32; jj++) lr[jj] = (lane < bs && jj < lane) ? lrow[jj] : T(0);
+            T wv = lane < bs ? S.w[b0 + lane] : T(0);
+#pragma unroll
+            for (int jj = 0; jj < 31; jj++) {
                 const T wj = __shfl_sync(0xffffffffu, wv, jj);
-                if (lane > jj && lane < bs) wv = fma(-lrow[jj], wj, wv);
+                if (lane > jj) wv = fma(-lr[jj], wj, wv);
             }
             if (lane < bs) S.w[b0 + lane] = wv;
         }
         __syncthreads();
-        for (int i = b0 + bs + warp; i < n; i += CTA_WARPS) {
-            T s = lane < bs ? A[(long long)i * lda + b0 + lane] * S.w[b0 + lane] : T(0);
-            s = warp_sum(s);
-            if (lane == 0) S.w[i] -= s;
-        }
+        cta_block_update(A + b0, lda, b0 + bs, n, b0, bs, S);
         __syncthreads();
     }
 }
@@ -716,15 +739,22 @@ __device__ int cta_upper_solve(const T *__restrict__ A, int lda, int n, CtaSmem<
     for (int b1 = n; b1 > 0; b1 -= 32) {
         const int b0 = max(0, b1 - 32), bs = b1 - b0;
         if (warp == 0) {
-            int bad = 0;
-            T wv = lane < bs ? S.w[b0 + lane] : T(0);
+            T ur[32];
             const T *urow = A + (long long)(b0 + lane) * lda + b0;
-            for (int jj = bs - 1; jj >= 0; jj--) {
-                const T d = A[(long long)(b0 + jj) * lda + b0 + jj];
-                if (absT(d) < tiny) bad = 1;
+#pragma unroll
+            for (int jj = 0; jj < 32; jj++) ur[jj] = (lane < bs && jj >= lane && jj < bs) ? urow[jj] : T(0);
+            T d = T(1);
+#pragma unroll
+            for (int jj = 0; jj < 32; jj++)
+                if (jj == lane) d = ur[jj];
+            const int bad = __any_sync(0xffffffffu, lane < bs && absT(d) < tiny);
+            T wv = lane < bs ? S.w[b0 + lane] : T(0);
+#pragma unroll
+            for (int jj = 31; jj >= 0; jj--) {
+                if (jj >= bs) continue;
                 if (lane == jj) wv = wv / d;
                 const T wj = __shfl_sync(0xffffffffu, wv, jj);
-                if (lane < jj) wv = fma(-urow[jj], wj, wv);
+                if (lane < jj) wv = fma(-ur[jj], wj, wv);
             }
             if (lane < bs) S.w[b0 + lane] = wv;
             if (lane == 0) S.status = bad;
@@ -734,11 +764,7 @@ __device__ int cta_upper_solve(const T *__restrict__ A, int lda, int n, CtaSmem<
             __syncthreads();
             return RL_ERR_DIV_BY_ZERO;
         }
-        for (int i = warp; i < b0; i += CTA_WARPS) {
-            T s = lane < bs ? A[(long long)i * lda + b0 + lane] * S.w[b0 + lane] : T(0);
-            s = warp_sum(s);
-            if (lane == 0) S.w[i] -= s;
-        }
+        cta_block_update(A + b0, lda, 0, b0, b0, bs, S);
         __syncthreads();
     }
     return RL_OK;
@@ -751,15 +777,22 @@ __device__ int cta_lower_solve(const T *__restrict__ A, int lda, int n, CtaSmem<
     for (int b0 = 0; b0 < n; b0 += 32) {
         const int bs = min(32, n - b0);
         if (warp == 0) {
-            int bad = 0;
-            T wv = lane < bs ? S.w[b0 + lane] : T(0);
+            T lr[32];
             const T *lrow = A + (long long)(b0 + lane) * lda + b0;
-            for (int jj = 0; jj < bs; jj++) {
-                const T d = A[(long long)(b0 + jj) * lda + b0 + jj];
-                if (absT(d) < tiny) bad = 1;
+#pragma unroll
+            for (int jj = 0; jj < 32; jj++) lr[jj] = (lane < bs && jj <= lane) ? lrow[jj] : T(0);
+            T d = T(1);
+#pragma unroll
+            for (int jj = 0; jj < 32; jj++)
+                if (jj == lane) d = lr[jj];
+            const int bad = __any_sync(0xffffffffu, lane < bs && absT(d) < tiny);
+            T wv = lane < bs ? S.w[b0 + lane] : T(0);
+#pragma unroll
+            for (int jj = 0; jj < 32; jj++) {
+                if (jj >= bs) break;
                 if (lane == jj) wv = wv / d;
                 const T wj = __shfl_sync(0xffffffffu, wv, jj);
-                if (lane > jj && lane < bs) wv = fma(-lrow[jj], wj, wv);
+                if (lane > jj) wv = fma(-lr[jj], wj, wv);
             }
             if (lane < bs) S.w[b0 + lane] = wv;
             if (lane == 0) S.status = bad;
@@ -769,11 +802,7 @@ __device__ int cta_lower_solve(const T *__restrict__ A, int lda, int n, CtaSmem<
             __syncthreads();
             return RL_ERR_DIV_BY_ZERO;
         }
-        for (int i = b0 + bs + warp; i < n; i += CTA_WARPS) {
-            T s = lane < bs ? A[(long long)i * lda + b0 + lane] * S.w[b0 + lane] : T(0);
-            s = warp_sum(s);
-            if (lane == 0) S.w[i] -= s;
-        }
+        cta_block_update(A + b0, lda, b0 + bs, n, b0, bs, S);
         __syncthreads();
     }
     return RL_OK;
@@ -786,15 +815,23 @@ __device__ int cta_lower_t_solve(const T *__restrict__ A, int lda, int n, CtaSme
     for (int b1 = n; b1 > 0; b1 -= 32) {
         const int b0 = max(0, b1 - 32), bs = b1 - b0;
         if (warp == 0) {
-            int bad = 0;
+            // lane holds column `lane` of the block of L^T, i.e. L[b0 + jj][b0 + lane]
+            T lc[32];
+#pragma unroll
+            for (int jj = 0; jj < 32; jj++)
+                lc[jj] = (lane < bs && jj < bs && jj >= lane) ? A[(long long)(b0 + jj) * lda + b0 + lane] : T(0);
+            T d = T(1);
+#pragma unroll
+            for (int jj = 0; jj < 32; jj++)
+                if (jj == lane) d = lc[jj];
+            const int bad = __any_sync(0xffffffffu, lane < bs && absT(d) < tiny);
             T wv = lane < bs ? S.w[b0 + lane] : T(0);
-            for (int jj = bs - 1; jj >= 0; jj--) {
-                const T *lrow = A + (long long)(b0 + jj) * lda + b0;  // row jj of L = column jj of L^T
-                const T d = lrow[jj];
-                if (absT(d) < tiny) bad = 1;
+#pragma unroll
+            for (int jj = 31; jj >= 0; jj--) {
+                if (jj >= bs) continue;
                 if (lane == jj) wv = wv / d;
                 const T wj = __shfl_sync(0xffffffffu, wv, jj);
-                if (lane < jj) wv = fma(-lrow[lane], wj, wv);
+                if (lane < jj) wv = fma(-lc[jj], wj, wv);
             }
             if (lane < bs) S.w[b0 + lane] = wv;
             if (lane == 0) S.status = bad;
@@ -804,9 +841,15 @@ __device__ int cta_lower_t_solve(const T *__restrict__ A, int lda, int n, CtaSme
             __syncthreads();
             return RL_ERR_DIV_BY_ZERO;
         }
+        // w[i] -= sum_jj L[b0 + jj][i] w[b0 + jj] for i < b0: a thread per i, coalesced rows
         for (int i = tid; i < b0; i += CTA_THREADS) {
+            T v[32];
+#pragma unroll
+            for (int jj = 0; jj < 32; jj++) v[jj] = jj < bs ? A[(long long)(b0 + jj) * lda + i] : T(0);
             T s = T(0);
-            for (int jj = 0; jj < bs; jj++) s = fma(A[(long long)(b0 + jj) * lda + i], S.w[b0 + jj], s);
+#pragma unroll
+            for (int jj = 0; jj < 32; jj++)
+                if (jj < bs) s = fma(v[jj], S.w[b0 + jj], s);
             S.w[i] -= s;
         }
         __syncthreads();
@@ -814,23 +857,45 @@ __device__ int cta_lower_t_solve(const T *__restrict__ A, int lda, int n, CtaSme
     return RL_OK;
 }
 
-// Applies LAPACK-style pivots (S.piv) to S.w in order.
+// Row permutation of an LU factorisation as a position -> original row map (from the
+// LAPACK-style pivots in S.piv), computed once per factorisation into S.rowperm.
 template <class T>
-__device__ void cta_apply_pivots(int n, CtaSmem<T> &S) {
+__device__ void cta_build_rowperm(int n, CtaSmem<T> &S) {
+    for (int i = threadIdx.x; i < n; i += CTA_THREADS) S.rowperm[i] = i;
+    __syncthreads();
     if (threadIdx.x == 0) {
         for (int j = 0; j < n; j++) {
             const int p = S.piv[j];
             if (p != j) {
-                const T t = S.w[j];
-                S.w[j] = S.w[p];
-                S.w[p] = t;
+                const int t = S.rowperm[j];
+                S.rowperm[j] = S.rowperm[p];
+                S.rowperm[p] = t;
             }
         }
     }
     __syncthreads();
 }
 
-// Full solve with a factor: kind 0 = LU (pivots in S.piv), 1 = Cholesky.
+// Applies the row permutation to S.w as a gather (through S.x's storage as scratch when
+// T is float; a second pass otherwise).
+template <class T>
+__device__ void cta_apply_pivots(int n, CtaSmem<T> &S) {
+    T v[CTA_NMAX / CTA_THREADS];
+#pragma unroll
+    for (int k = 0; k < CTA_NMAX / CTA_THREADS; k++) {
+        const int i = threadIdx.x + k * CTA_THREADS;
+        v[k] = i < n ? S.w[S.rowperm[i]] : T(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < CTA_NMAX / CTA_THREADS; k++) {
+        const int i = threadIdx.x + k * CTA_THREADS;
+        if (i < n) S.w[i] = v[k];
+    }
+    __syncthreads();
+}
+
+// Full solve with a factor: kind 0 = LU (row permutation in S.rowperm), 1 = Cholesky.
 template <class T>
 __device__ int cta_factor_solve(const T *A, int lda, int n, int kind, CtaSmem<T> &S, T tiny) {
     if (kind == 1) {
