@@ -50,6 +50,12 @@ def parse():
                    help="CPU baseline sample size in GFLOP of factorisation work")
     p.add_argument("--skip-e2e", action="store_true")
     p.add_argument("--skip-cpu", action="store_true")
+    p.add_argument("--workload", default="batch", choices=["batch", "dense", "mixed", "serve"],
+                   help="batch: the headline batched mix (default); dense: GEMM sweep n=1024..8192 f32/f64 "
+                        "and plain FP64 LU; mixed: single-system mixed precision vs FP64 over n and kappa; "
+                        "serve: Poisson request stream through the serving loop")
+    p.add_argument("--sizes", default="", help="comma-separated sizes for dense / mixed")
+    p.add_argument("--lambdas", default="1000,10000,50000", help="serve: arrival rates (requests/s)")
     return p.parse_args()
 
 
@@ -172,6 +178,220 @@ def reference_arm(args, rank, world):
     }), flush=True)
 
 
+def event_times(fn, steps, warmup, stream, flush=None):
+    """CUDA-event times (ms) of `steps` calls of fn on `stream`, after `warmup` calls; when
+    `flush` is given it is overwritten before every call (L2 flush, outside the events)."""
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    out = []
+    for _ in range(steps):
+        if flush is not None:
+            flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        out.append(e0.elapsed_time(e1))
+    return out
+
+
+def dense_workload(args, rank, world, dev):
+    """GEMM sweep (f32 / f64, n = 1024 .. 8192) and plain FP64 LU solves: TFLOP/s against
+    the measured FP64 and FP32 peaks, cuBLAS (torch.matmul) beside it for context, and
+    the accuracy bound n eps ||A|| ||B|| (inf-norms) checked against an FP64 product."""
+    import torch
+    import rulinalg_gb300 as rl
+    from rulinalg_gb300.workloads import config1_lu
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    sizes = [int(x) for x in args.sizes.split(",")] if args.sizes else [1024, 2048, 4096, 8192]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    steps, warm = max(1, args.steps), max(3, args.warmup)
+    sweep = []
+    l0 = rl.launch_count()
+    with ClockSampler(dev.index or 0) as clk:
+        for n in sizes:
+            g = torch.Generator(device=dev)
+            g.manual_seed(n)
+            a64 = torch.randn(n, n, dtype=torch.float64, device=dev, generator=g)
+            b64 = torch.randn(n, n, dtype=torch.float64, device=dev, generator=g)
+            ref = a64 @ b64
+            bound_base = float(a64.abs().sum(1).max() * b64.abs().sum(1).max())
+            for dt, fn_name, eps in ((torch.float32, "rl_sgemm_dev", 2.0 ** -24), (torch.float64, "rl_dgemm_dev", U64)):
+                a, b = a64.to(dt), b64.to(dt)
+                c = torch.empty(n, n, dtype=dt, device=dev)
+                f = getattr(rl.lib, fn_name)
+                call = lambda: f(n, n, n, a.data_ptr(), n, b.data_ptr(), n, c.data_ptr(), n, sh)
+                ms = event_times(call, steps, warm, stream, flush)
+                err = float((c.double() - (a.double() @ b.double())).abs().max())
+                cub = event_times(lambda: torch.matmul(a, b, out=c), steps, warm, stream, flush)
+                t = statistics.median(ms) / 1e3
+                sweep.append({"op": "gemm", "n": n, "dtype": "f32" if dt == torch.float32 else "f64",
+                              "ms": statistics.median(ms), "tflops": 2.0 * n ** 3 / t / 1e12,
+                              "cublas_tflops": 2.0 * n ** 3 / (statistics.median(cub) / 1e3) / 1e12,
+                              "max_abs_err": err, "bound": n * eps * bound_base,
+                              "within": err <= n * eps * bound_base})
+            del a64, b64, ref
+        # plain FP64 LU factor + solve (PartialPivLu in FP64, one right-hand side)
+        for n in ([1024] + [s for s in sizes if s >= 4096]):
+            a_h, x_true, b_h = config1_lu(n, seed=0)
+            a = torch.from_numpy(a_h).to(dev)
+            b = torch.from_numpy(b_h).to(dev).reshape(n, 1)
+            x = torch.empty_like(b)
+            call = lambda: rl.lib.rl_dsolve_fp64_dev(n, 1, 0, a.data_ptr(), n, b.data_ptr(), 1, x.data_ptr(), 1,
+                                                     None, sh)
+            ms = event_times(call, max(1, steps // 2), 1, stream, flush)
+            t = statistics.median(ms) / 1e3
+            r = (b - a @ x).abs().max().item()
+            berr = r / (a.abs().sum(1).max().item() * x.abs().max().item() + b.abs().max().item())
+            sweep.append({"op": "lu_fp64_solve", "n": n, "dtype": "f64", "ms": statistics.median(ms),
+                          "tflops": (2.0 * n ** 3 / 3.0 + 2.0 * n * n) / t / 1e12, "berr": berr,
+                          "within": berr <= n * U64 * 10, "x_err": float(np.abs(x.cpu().numpy()[:, 0] - x_true).max())})
+    launches = rl.launch_count() - l0
+    head = next((r for r in sweep if r["op"] == "gemm" and r["dtype"] == "f64" and r["n"] == max(sizes)), sweep[0])
+    fp64_peak = 1.05
+    line = {
+        "metric": f"FP64 GEMM TFLOP/s (n={head['n']})", "value": head["tflops"], "unit": "TFLOP/s", "n_gpus": world,
+        "steps": steps, "warmup": warm, "ms_per_step": head["ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "square GEMM sweep f32/f64 + plain FP64 LU solve", "sizes": sizes,
+                   "l2": "256 MB buffer overwritten before every timed call"},
+        "roofline": {"bound": "fp64 pipe", "achieved": head["tflops"], "peak": fp64_peak, "unit": "TFLOP/s",
+                     "frac": head["tflops"] / fp64_peak, "traffic": None,
+                     "peak_source": "FP64 DMMA/DFMA probe on this GB300 (MEASURED_PEAKS.json holds no FP64 figure)"},
+        "sweep": sweep, "gpu_launches": launches, "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def mixed_workload(args, rank, world, dev):
+    """Single large systems: mixed-precision solve (FP32 factor, FP64 refinement,
+    GMRES-IR, FP64 refactor) against the plain FP64 GPU solve, A = U diag(sigma) V^T with
+    Haar U, V and geometric sigma (condition number kappa), nrhs N(0,1) columns."""
+    import torch
+    import rulinalg_gb300 as rl
+    from rulinalg_gb300._lib import SolveInfo
+    import ctypes as C
+    from rulinalg_gb300.workloads import conditioned_system
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    sizes = [int(x) for x in args.sizes.split(",")] if args.sizes else [4096, 8192, 16384]
+    kappas = [1e2, 1e6, 1e10]
+    cases = []
+    l0 = rl.launch_count()
+    paths = {0: "refinement", 1: "gmres-ir", 2: "fp64"}
+    with ClockSampler(dev.index or 0) as clk:
+        for n in sizes:
+            reps = 3 if n <= 8192 else 1
+            for kappa in kappas:
+                a, bfull = conditioned_system(n, kappa, 64, seed=n, device=dev)
+                for nrhs in (1, 64):
+                    b = bfull[:, :nrhs].contiguous()
+                    x = torch.empty_like(b)
+                    row = {"n": n, "kappa": kappa, "nrhs": nrhs}
+                    for name, fn in (("mixed", rl.lib.rl_dsolve_mixed_dev), ("fp64", rl.lib.rl_dsolve_fp64_dev)):
+                        info = SolveInfo()
+                        call = lambda: fn(n, nrhs, 0, a.data_ptr(), n, b.data_ptr(), nrhs, x.data_ptr(), nrhs,
+                                          C.byref(info), sh)
+                        ms = event_times(call, reps, 1, stream)
+                        row[name] = {"ms": statistics.median(ms), "berr": info.berr, "iters": info.iters,
+                                     "gmres_iters": info.gmres_iters, "path": paths.get(info.path, info.path),
+                                     "within": info.berr <= n * U64 * 10}
+                    row["speedup"] = row["fp64"]["ms"] / row["mixed"]["ms"]
+                    cases.append(row)
+                del a, bfull
+    launches = rl.launch_count() - l0
+    sp = [c["speedup"] for c in cases]
+    geo = float(np.exp(np.mean(np.log(sp))))
+    line = {
+        "metric": "mixed-precision / plain FP64 single-system solve speedup at equal backward error (geomean)",
+        "value": geo, "unit": "x", "n_gpus": world, "steps": 1, "warmup": 1,
+        "ms_per_step": float(np.mean([c["mixed"]["ms"] for c in cases])), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 factor + f64 refinement", "data": "synthetic",
+        "config": {"workload": "A = U diag(sigma) V^T, Haar U, V", "sizes": sizes, "kappas": kappas, "nrhs": [1, 64],
+                   "l2": "inputs 128 MB+ per matrix > L2"},
+        "cases": cases, "all_within": all(c["mixed"]["within"] for c in cases),
+        "gpu_launches": launches, "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def serve_workload(args, rank, world, dev):
+    """A Poisson request stream through the serving loop: sizes log-uniform in [16, 4096];
+    70% fresh systems (50% LU, 30% Cholesky, 20% QR least squares with m = 2n) and 30%
+    re-solves against resident LU factors. Systems come from a seeded pool that the
+    requests cycle through (the host arrays are read-only; each request has its own x)."""
+    import rulinalg_gb300 as rl
+    from rulinalg_gb300.workloads import log_uniform_sizes
+    rng = np.random.default_rng(args.seed)
+    pool = {0: [], 1: [], 2: []}
+    per_kind = 24
+    for kind in (0, 1, 2):
+        for n in log_uniform_sizes(per_kind, 16, 4096, rng):
+            n = int(n)
+            if kind == 0:
+                a = rng.uniform(-1, 1, (n, n)) + n * np.eye(n)
+            elif kind == 1:
+                u = rng.uniform(-1, 1, (n, n))
+                a = 0.5 * (u + u.T) + n * np.eye(n)
+            else:
+                a = rng.standard_normal((2 * n, n))
+            pool[kind].append((a, rng.standard_normal(a.shape[0])))
+    srv = rl.Server()
+    resident = []
+    for n in log_uniform_sizes(8, 16, 4096, rng):
+        n = int(n)
+        a = rng.uniform(-1, 1, (n, n)) + n * np.eye(n)
+        t, _ = srv.submit(rl.REQ_LU, a, rng.standard_normal(n), retain=True)
+        r = srv.wait(t)
+        resident.append((r["factor"], n))
+    lambdas = [float(x) for x in args.lambdas.split(",")]
+    runs = []
+    with ClockSampler(dev.index or 0) as clk:
+        for lam in lambdas:
+            count = int(min(4000, max(1000, lam * 0.5)))
+            arrivals = np.cumsum(rng.exponential(1.0 / lam, count))
+            reqs = []
+            for i in range(count):
+                if rng.random() < 0.3:
+                    h, n = resident[int(rng.integers(len(resident)))]
+                    reqs.append((rl.REQ_RESOLVE, None, rng.standard_normal(n), h))
+                else:
+                    kind = int(rng.choice(3, p=[0.5, 0.3, 0.2]))
+                    a, b = pool[kind][int(rng.integers(per_kind))]
+                    reqs.append(({0: rl.REQ_LU, 1: rl.REQ_CHOLESKY, 2: rl.REQ_LSTSQ}[kind], a, b, 0))
+            srv.reset_stats()
+            t0 = time.perf_counter()
+            res = srv.replay(arrivals, reqs)
+            wall = time.perf_counter() - t0
+            st = srv.stats()
+            ok = sum(1 for r in res if r["status"] == 0)
+            berrs = [r["berr"] for r, q in zip(res, reqs) if q[0] != rl.REQ_LSTSQ]
+            runs.append({"lambda": lam, "requests": count, "ok": ok, "p50_ms": st["p50_us"] / 1e3,
+                         "p99_ms": st["p99_us"] / 1e3, "mean_ms": st["mean_us"] / 1e3,
+                         "solves_per_s": st["solves_per_s"], "wall_s": wall, "batches": st["batches"],
+                         "batched_requests": st["batched_requests"], "bytes_peak": st["bytes_peak"],
+                         "max_berr": max(berrs) if berrs else None})
+    srv.close()
+    head = runs[0]
+    line = {
+        "metric": f"served solves/s and p99 latency (Poisson, lambda={int(head['lambda'])}/s)",
+        "value": head["solves_per_s"], "unit": "solves/s", "n_gpus": world, "steps": len(runs), "warmup": 0,
+        "ms_per_step": head["p99_ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 factor + f64 refinement (LU/Cholesky), f64 (QR)", "data": "synthetic",
+        "config": {"workload": "served stream: sizes log-uniform [16,4096], 50% LU / 30% Cholesky / 20% QR LS "
+                               "(m=2n), 30% re-solves", "pool_per_kind": per_kind, "resident_factors": len(resident)},
+        "runs": runs, "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -190,6 +410,13 @@ def main():
     torch.cuda.set_device(dev)
     if not rl.device_available():
         raise SystemExit("rulinalg_gb300: no usable sm_103 GPU")
+    other = {"dense": dense_workload, "mixed": mixed_workload, "serve": serve_workload}.get(args.workload)
+    if other is not None:
+        other(args, rank, world, dev)
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
     n, kind, a, b = mixed_batch(args.count_spd, args.count_lu, seed=args.seed, device=dev)
     count = len(n)
     stream = torch.cuda.current_stream()

@@ -56,7 +56,7 @@ __device__ void push_fallback(const BatchDesc &d, int sys) {
 template <class TI, class TF, bool MIXED>
 __device__ void batch_solve_one(const BatchDesc &d, int sys, const TI *__restrict__ A, const TI *__restrict__ B,
                                 TI *__restrict__ X, TF *__restrict__ W, CtaSmem<TF> &S) {
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tid = threadIdx.x;
     const int n = d.n[sys];
     const int kind = d.kind[sys];
     const TI *Ai = A + d.a_off[sys];
@@ -70,20 +70,7 @@ __device__ void batch_solve_one(const BatchDesc &d, int sys, const TI *__restric
     // Working copy in the factor type (row stride rounded up to 4 elements so that the
     // trailing updates use 128-bit accesses); ||A||_inf from the same pass.
     const int ldw = (n + 3) & ~3;
-    double rowmax = 0.0;
-    for (int i = warp; i < n; i += CTA_WARPS) {
-        const TI *row = Ai + (long long)i * n;
-        TF *wrow = W + (long long)i * ldw;
-        TF s = TF(0);
-        for (int j = lane; j < n; j += 32) {
-            const TF v = (TF)row[j];
-            wrow[j] = v;
-            s += absT(v);
-        }
-        s = warp_sum(s);
-        rowmax = fmax(rowmax, (double)s);
-    }
-    const double anorm = block_max(rowmax, S);
+    const double anorm = cta_copy_convert<TI, TF>(Ai, n, n, W, ldw, S);
     double bm = 0.0;
     for (int i = tid; i < n; i += CTA_THREADS) bm = fmax(bm, fabs((double)bi[i]));
     const double bnorm = block_max(bm, S);

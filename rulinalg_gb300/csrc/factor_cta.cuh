@@ -908,23 +908,113 @@ __device__ int cta_factor_solve(const T *A, int lda, int n, int kind, CtaSmem<T>
     return cta_upper_solve(A, lda, n, S, tiny);
 }
 
-// FP64 residual S.r = b - A S.x for the original matrix (type TI, row stride lda);
-// returns max |r_i| (uniform).
-template <class TI, class T>
-__device__ double cta_residual(const TI *__restrict__ A, int lda, const TI *__restrict__ b, int n,
-                               CtaSmem<T> &S) {
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+// Row-block passes over an n x n row-major matrix: a warp covers R = 16 / C consecutive
+// rows x 32 C columns per pass (lane owns columns lane + 32 c), so every lane keeps 16
+// loads in flight whatever n is. C is picked from n (n <= 32 C).
+template <int C, class TI, class TF>
+__device__ double copy_rows(const TI *__restrict__ A, int lda, int n, TF *__restrict__ W, int ldw) {
+    constexpr int R = 16 / C;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     double mx = 0.0;
-    for (int i = warp; i < n; i += CTA_WARPS) {
-        const TI *row = A + (long long)i * lda;
-        double s = 0.0;
-        for (int j = lane; j < n; j += 32) s = fma((double)row[j], S.x[j], s);
-        s = warp_sum(s);
-        const double ri = (double)b[i] - s;
-        if (lane == 0) S.r[i] = ri;
-        mx = fmax(mx, fabs(ri));
+    for (int i0 = warp * R; i0 < n; i0 += CTA_WARPS * R) {
+        TI v[R][C];
+#pragma unroll
+        for (int r = 0; r < R; r++)
+#pragma unroll
+            for (int c = 0; c < C; c++) {
+                const int i = i0 + r, j = lane + 32 * c;
+                v[r][c] = (i < n && j < n) ? A[(long long)i * lda + j] : TI(0);
+            }
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int i = i0 + r;
+            TF s = TF(0);
+#pragma unroll
+            for (int c = 0; c < C; c++) {
+                const int j = lane + 32 * c;
+                const TF f = (TF)v[r][c];
+                if (i < n && j < n) W[(long long)i * ldw + j] = f;
+                s += absT(f);
+            }
+            s = warp_sum(s);
+            mx = fmax(mx, (double)s);
+        }
     }
-    (void)tid;
+    return mx;
+}
+
+// Copies A (TI, row stride lda) into the factor workspace W (TF, row stride ldw) and
+// returns ||A||_inf of the converted copy (uniform).
+template <class TI, class TF>
+__device__ double cta_copy_convert(const TI *__restrict__ A, int lda, int n, TF *__restrict__ W, int ldw,
+                                   CtaSmem<TF> &S) {
+    double mx;
+    if (n > 256)
+        mx = copy_rows<16>(A, lda, n, W, ldw);
+    else if (n > 128)
+        mx = copy_rows<8>(A, lda, n, W, ldw);
+    else if (n > 64)
+        mx = copy_rows<4>(A, lda, n, W, ldw);
+    else if (n > 32)
+        mx = copy_rows<2>(A, lda, n, W, ldw);
+    else
+        mx = copy_rows<1>(A, lda, n, W, ldw);
+    return block_max(mx, S);
+}
+
+template <int C, class TI, class T>
+__device__ double residual_rows(const TI *__restrict__ A, int lda, const TI *__restrict__ b, int n, CtaSmem<T> &S) {
+    constexpr int R = 16 / C;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double xr[C];
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+        const int j = lane + 32 * c;
+        xr[c] = j < n ? S.x[j] : 0.0;
+    }
+    double mx = 0.0;
+    for (int i0 = warp * R; i0 < n; i0 += CTA_WARPS * R) {
+        TI v[R][C];
+#pragma unroll
+        for (int r = 0; r < R; r++)
+#pragma unroll
+            for (int c = 0; c < C; c++) {
+                const int i = i0 + r, j = lane + 32 * c;
+                v[r][c] = (i < n && j < n) ? A[(long long)i * lda + j] : TI(0);
+            }
+        const double bl = (lane < R && i0 + lane < n) ? (double)b[i0 + lane] : 0.0;
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            double s = 0.0;
+#pragma unroll
+            for (int c = 0; c < C; c++) s = fma((double)v[r][c], xr[c], s);
+            s = warp_sum(s);
+            const double ri = __shfl_sync(0xffffffffu, bl, r) - s;
+            if (i0 + r < n) {
+                if (lane == 0) S.r[i0 + r] = ri;
+                mx = fmax(mx, fabs(ri));
+            }
+        }
+    }
+    return mx;
+}
+
+// FP64 residual S.r = b - A S.x for the original matrix (type TI, row stride lda);
+// returns max |r_i| (uniform). Each lane sums its columns j = lane, lane + 32, ... in
+// order, then the warp tree adds the lanes.
+template <class TI, class T>
+__device__ double cta_residual(const TI *__restrict__ A, int lda, const TI *__restrict__ b, int n, CtaSmem<T> &S) {
+    double mx;
+    if (n > 256)
+        mx = residual_rows<16>(A, lda, b, n, S);
+    else if (n > 128)
+        mx = residual_rows<8>(A, lda, b, n, S);
+    else if (n > 64)
+        mx = residual_rows<4>(A, lda, b, n, S);
+    else if (n > 32)
+        mx = residual_rows<2>(A, lda, b, n, S);
+    else
+        mx = residual_rows<1>(A, lda, b, n, S);
     return block_max(mx, S);
 }
 

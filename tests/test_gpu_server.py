@@ -43,13 +43,12 @@ def test_same_alone_and_in_the_mix(gpu, server):
         a, b = system(rng, kind, int(rng.integers(8, 300)))
         tickets.append(server.submit(kind, a, b)[0])
         if i % 60 == 30:
-            for kind2, a2, b2 in probes:
-                tickets.append(("probe", server.submit(kind2, a2, b2)[0]))
+            for p_i, (kind2, a2, b2) in enumerate(probes):
+                tickets.append((p_i, server.submit(kind2, a2, b2)[0]))
     mixed = {}
     for t in tickets:
         if isinstance(t, tuple):
-            r = server.wait(t[1])
-            mixed.setdefault(len(mixed) % len(probes), []).append(r)
+            mixed.setdefault(t[0], []).append(server.wait(t[1]))
         else:
             assert server.wait(t)["status"] == 0
     for p_i, (kind, a, b) in enumerate(probes):
