@@ -682,41 +682,81 @@ __device__ int cta_chol_factor(T *__restrict__ A, int lda, int n, CtaSmem<T> &S,
 }
 
 // ------------------------------------------------------------------------- solves --
-// In-place solves on the shared vector S.w. Triangles are read from global memory (the
-// factor lives in L2): each 32 x 32 diagonal block by warp 0, every lane holding its
-// block row in registers (loaded up front, all loads in flight) and the solution moving
-// by shuffles; the off-block updates with a thread per row (or per column for L^T), its
-// 32 loads issued together.
+// In-place solves on the shared vector S.w, 32 x 32 blocks at a time. Triangles are read
+// from global memory (the factor lives in L2) with coalesced row segments only: warp 0
+// stages each diagonal block through a padded shared tile so that every lane holds its
+// block row, the solution moving by shuffles; the off-block updates take 32 rows per
+// warp, lane c reading column c, and a butterfly reduce-scatter leaves row r's sum in
+// lane r.
 
-// w[i] -= sum_{j < bs} M[i][j] * w[b0 + j] for the rows i in [lo, hi) of M (M points at
+// w[i] -= sum_{c < bs} M[i][c] * w[b0 + c] for the rows i in [lo, hi) of M (M points at
 // column b0 of row 0; row stride lda).
 template <class T>
 __device__ __forceinline__ void cta_block_update(const T *__restrict__ M, int lda, int lo, int hi, int b0, int bs,
                                                  CtaSmem<T> &S) {
-    for (int i = lo + threadIdx.x; i < hi; i += CTA_THREADS) {
-        const T *row = M + (long long)i * lda;
-        T v[32];
+    constexpr int RB = sizeof(T) == 4 ? 32 : 16;  // rows per warp pass
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const T y = lane < bs ? S.w[b0 + lane] : T(0);
+    for (int r0 = lo + warp * RB; r0 < hi; r0 += CTA_WARPS * RB) {
+        T p[RB];
 #pragma unroll
-        for (int j = 0; j < 32; j++) v[j] = j < bs ? row[j] : T(0);
-        T s = T(0);
+        for (int r = 0; r < RB; r++) {
+            const int i = r0 + r;
+            p[r] = (i < hi && lane < bs) ? M[(long long)i * lda + lane] : T(0);
+        }
 #pragma unroll
-        for (int j = 0; j < 32; j++)
-            if (j < bs) s = fma(v[j], S.w[b0 + j], s);
-        S.w[i] -= s;
+        for (int r = 0; r < RB; r++) p[r] *= y;
+#pragma unroll
+        for (int s = 16; s >= RB; s >>= 1)
+#pragma unroll
+            for (int r = 0; r < RB; r++) p[r] += __shfl_xor_sync(0xffffffffu, p[r], s);
+#pragma unroll
+        for (int s = RB / 2; s >= 1; s >>= 1) {
+            const bool up = lane & s;
+#pragma unroll
+            for (int k = 0; k < s; k++) {
+                const T send = up ? p[k] : p[k + s];
+                const T keep = up ? p[k + s] : p[k];
+                p[k] = keep + __shfl_xor_sync(0xffffffffu, send, s);
+            }
+        }
+        const int i = r0 + (lane & (RB - 1));
+        if (lane < RB && i < hi) S.w[i] -= p[0];
     }
+}
+
+// Warp 0: lane r receives row b0 + r of the diagonal block (columns b0 .. b0 + bs),
+// loaded as coalesced row segments and transposed through a padded tile in S.P.
+template <class T>
+__device__ __forceinline__ void load_diag_rows(const T *__restrict__ A, int lda, int b0, int bs, T (&d)[32],
+                                               CtaSmem<T> &S) {
+    const int lane = threadIdx.x & 31;
+    T v[32];
+#pragma unroll
+    for (int r = 0; r < 32; r++) v[r] = (r < bs && lane < bs) ? A[(long long)(b0 + r) * lda + b0 + lane] : T(0);
+#pragma unroll
+    for (int r = 0; r < 32; r++) S.P[r * 33 + lane] = v[r];
+    __syncwarp();
+#pragma unroll
+    for (int c = 0; c < 32; c++) d[c] = S.P[lane * 33 + c];
+    __syncwarp();
+}
+
+// 1 / d for the factor type's solves: FP32 multiplies by the reciprocal, FP64 divides.
+template <class T>
+__device__ __forceinline__ T solve_div(T v, T d, T inv) {
+    return sizeof(T) == 8 ? v / d : v * inv;
 }
 
 // Unit lower triangular solve L y = w (L strictly below the diagonal of A).
 template <class T>
 __device__ void cta_unit_lower_solve(const T *__restrict__ A, int lda, int n, CtaSmem<T> &S) {
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int b0 = 0; b0 < n; b0 += 32) {
         const int bs = min(32, n - b0);
         if (warp == 0) {
             T lr[32];
-            const T *lrow = A + (long long)(b0 + lane) * lda + b0;
-#pragma unroll
-            for (int jj = 0; jj < 32; jj++) lr[jj] = (lane < bs && jj < lane) ? lrow[jj] : T(0);
+            load_diag_rows(A, lda, b0, bs, lr, S);
             T wv = lane < bs ? S.w[b0 + lane] : T(0);
 #pragma unroll
             for (int jj = 0; jj < 31; jj++) {
@@ -735,24 +775,23 @@ __device__ void cta_unit_lower_solve(const T *__restrict__ A, int lda, int n, Ct
 // returns RL_ERR_DIV_BY_ZERO (src/matrix/mod.rs:333-336).
 template <class T>
 __device__ int cta_upper_solve(const T *__restrict__ A, int lda, int n, CtaSmem<T> &S, T tiny) {
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int b1 = n; b1 > 0; b1 -= 32) {
         const int b0 = max(0, b1 - 32), bs = b1 - b0;
         if (warp == 0) {
             T ur[32];
-            const T *urow = A + (long long)(b0 + lane) * lda + b0;
-#pragma unroll
-            for (int jj = 0; jj < 32; jj++) ur[jj] = (lane < bs && jj >= lane && jj < bs) ? urow[jj] : T(0);
+            load_diag_rows(A, lda, b0, bs, ur, S);
             T d = T(1);
 #pragma unroll
             for (int jj = 0; jj < 32; jj++)
                 if (jj == lane) d = ur[jj];
             const int bad = __any_sync(0xffffffffu, lane < bs && absT(d) < tiny);
+            const T inv = T(1) / d;
             T wv = lane < bs ? S.w[b0 + lane] : T(0);
 #pragma unroll
             for (int jj = 31; jj >= 0; jj--) {
                 if (jj >= bs) continue;
-                if (lane == jj) wv = wv / d;
+                if (lane == jj) wv = solve_div(wv, d, inv);
                 const T wj = __shfl_sync(0xffffffffu, wv, jj);
                 if (lane < jj) wv = fma(-ur[jj], wj, wv);
             }
@@ -773,24 +812,23 @@ __device__ int cta_upper_solve(const T *__restrict__ A, int lda, int n, CtaSmem<
 // Lower (non-unit) solve L y = w; |l_ii| < tiny -> RL_ERR_DIV_BY_ZERO (mod.rs:375-378).
 template <class T>
 __device__ int cta_lower_solve(const T *__restrict__ A, int lda, int n, CtaSmem<T> &S, T tiny) {
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int b0 = 0; b0 < n; b0 += 32) {
         const int bs = min(32, n - b0);
         if (warp == 0) {
             T lr[32];
-            const T *lrow = A + (long long)(b0 + lane) * lda + b0;
-#pragma unroll
-            for (int jj = 0; jj < 32; jj++) lr[jj] = (lane < bs && jj <= lane) ? lrow[jj] : T(0);
+            load_diag_rows(A, lda, b0, bs, lr, S);
             T d = T(1);
 #pragma unroll
             for (int jj = 0; jj < 32; jj++)
                 if (jj == lane) d = lr[jj];
             const int bad = __any_sync(0xffffffffu, lane < bs && absT(d) < tiny);
+            const T inv = T(1) / d;
             T wv = lane < bs ? S.w[b0 + lane] : T(0);
 #pragma unroll
             for (int jj = 0; jj < 32; jj++) {
                 if (jj >= bs) break;
-                if (lane == jj) wv = wv / d;
+                if (lane == jj) wv = solve_div(wv, d, inv);
                 const T wj = __shfl_sync(0xffffffffu, wv, jj);
                 if (lane > jj) wv = fma(-lr[jj], wj, wv);
             }
@@ -825,11 +863,12 @@ __device__ int cta_lower_t_solve(const T *__restrict__ A, int lda, int n, CtaSme
             for (int jj = 0; jj < 32; jj++)
                 if (jj == lane) d = lc[jj];
             const int bad = __any_sync(0xffffffffu, lane < bs && absT(d) < tiny);
+            const T inv = T(1) / d;
             T wv = lane < bs ? S.w[b0 + lane] : T(0);
 #pragma unroll
             for (int jj = 31; jj >= 0; jj--) {
                 if (jj >= bs) continue;
-                if (lane == jj) wv = wv / d;
+                if (lane == jj) wv = solve_div(wv, d, inv);
                 const T wj = __shfl_sync(0xffffffffu, wv, jj);
                 if (lane < jj) wv = fma(-lc[jj], wj, wv);
             }
@@ -908,12 +947,12 @@ __device__ int cta_factor_solve(const T *A, int lda, int n, int kind, CtaSmem<T>
     return cta_upper_solve(A, lda, n, S, tiny);
 }
 
-// Row-block passes over an n x n row-major matrix: a warp covers R = 16 / C consecutive
-// rows x 32 C columns per pass (lane owns columns lane + 32 c), so every lane keeps 16
-// loads in flight whatever n is. C is picked from n (n <= 32 C).
-template <int C, class TI, class TF>
+// Row-block passes over an n x n row-major matrix: a warp covers R consecutive rows x
+// 32 C columns per pass (lane owns columns lane + 32 c), every lane issuing its R C
+// loads before using any. (C, R) is picked from n (n <= 32 C) so that a lane keeps 16 to
+// 32 loads in flight.
+template <int C, int R, class TI, class TF>
 __device__ double copy_rows(const TI *__restrict__ A, int lda, int n, TF *__restrict__ W, int ldw) {
-    constexpr int R = 16 / C;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     double mx = 0.0;
     for (int i0 = warp * R; i0 < n; i0 += CTA_WARPS * R) {
@@ -950,28 +989,21 @@ __device__ double cta_copy_convert(const TI *__restrict__ A, int lda, int n, TF 
                                    CtaSmem<TF> &S) {
     double mx;
     if (n > 256)
-        mx = copy_rows<16>(A, lda, n, W, ldw);
+        mx = copy_rows<16, 2>(A, lda, n, W, ldw);
     else if (n > 128)
-        mx = copy_rows<8>(A, lda, n, W, ldw);
+        mx = copy_rows<8, 4>(A, lda, n, W, ldw);
     else if (n > 64)
-        mx = copy_rows<4>(A, lda, n, W, ldw);
+        mx = copy_rows<4, 4>(A, lda, n, W, ldw);
     else if (n > 32)
-        mx = copy_rows<2>(A, lda, n, W, ldw);
+        mx = copy_rows<2, 4>(A, lda, n, W, ldw);
     else
-        mx = copy_rows<1>(A, lda, n, W, ldw);
+        mx = copy_rows<1, 4>(A, lda, n, W, ldw);
     return block_max(mx, S);
 }
 
-template <int C, class TI, class T>
+template <int C, int R, class TI, class T>
 __device__ double residual_rows(const TI *__restrict__ A, int lda, const TI *__restrict__ b, int n, CtaSmem<T> &S) {
-    constexpr int R = 16 / C;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double xr[C];
-#pragma unroll
-    for (int c = 0; c < C; c++) {
-        const int j = lane + 32 * c;
-        xr[c] = j < n ? S.x[j] : 0.0;
-    }
     double mx = 0.0;
     for (int i0 = warp * R; i0 < n; i0 += CTA_WARPS * R) {
         TI v[R][C];
@@ -987,7 +1019,10 @@ __device__ double residual_rows(const TI *__restrict__ A, int lda, const TI *__r
         for (int r = 0; r < R; r++) {
             double s = 0.0;
 #pragma unroll
-            for (int c = 0; c < C; c++) s = fma((double)v[r][c], xr[c], s);
+            for (int c = 0; c < C; c++) {
+                const int j = lane + 32 * c;
+                s = fma((double)v[r][c], j < n ? S.x[j] : 0.0, s);
+            }
             s = warp_sum(s);
             const double ri = __shfl_sync(0xffffffffu, bl, r) - s;
             if (i0 + r < n) {
@@ -1006,15 +1041,15 @@ template <class TI, class T>
 __device__ double cta_residual(const TI *__restrict__ A, int lda, const TI *__restrict__ b, int n, CtaSmem<T> &S) {
     double mx;
     if (n > 256)
-        mx = residual_rows<16>(A, lda, b, n, S);
+        mx = residual_rows<16, 2>(A, lda, b, n, S);
     else if (n > 128)
-        mx = residual_rows<8>(A, lda, b, n, S);
+        mx = residual_rows<8, 4>(A, lda, b, n, S);
     else if (n > 64)
-        mx = residual_rows<4>(A, lda, b, n, S);
+        mx = residual_rows<4, 4>(A, lda, b, n, S);
     else if (n > 32)
-        mx = residual_rows<2>(A, lda, b, n, S);
+        mx = residual_rows<2, 4>(A, lda, b, n, S);
     else
-        mx = residual_rows<1>(A, lda, b, n, S);
+        mx = residual_rows<1, 4>(A, lda, b, n, S);
     return block_max(mx, S);
 }
 
