@@ -34,7 +34,7 @@ template <class T>
 struct CtaNB;
 template <>
 struct CtaNB<float> {
-    static constexpr int value = 32;
+    static constexpr int value = 16;
 };
 template <>
 struct CtaNB<double> {
@@ -684,16 +684,15 @@ __device__ int cta_chol_factor(T *__restrict__ A, int lda, int n, CtaSmem<T> &S,
 // ------------------------------------------------------------------------- solves --
 // In-place solves on the shared vector S.w, 32 x 32 blocks at a time. Triangles are read
 // from global memory (the factor lives in L2) with coalesced row segments only: warp 0
-// stages each diagonal block through a padded shared tile so that every lane holds its
-// block row, the solution moving by shuffles; the off-block updates take 32 rows per
-// warp, lane c reading column c, and a butterfly reduce-scatter leaves row r's sum in
-// lane r.
+// stages each diagonal block in a padded shared tile and solves it with the solution
+// moving by shuffles; the off-block updates take 32 rows per warp (16 for FP64), lane c
+// reading column c, and a butterfly reduce-scatter leaves row r's sum in lane r.
 
 // w[i] -= sum_{c < bs} M[i][c] * w[b0 + c] for the rows i in [lo, hi) of M (M points at
 // column b0 of row 0; row stride lda).
 template <class T>
-__device__ __forceinline__ void cta_block_update(const T *__restrict__ M, int lda, int lo, int hi, int b0, int bs,
-                                                 CtaSmem<T> &S) {
+__device__ __noinline__ void cta_block_update(const T *__restrict__ M, int lda, int lo, int hi, int b0, int bs,
+                                              CtaSmem<T> &S) {
     constexpr int RB = sizeof(T) == 4 ? 32 : 16;  // rows per warp pass
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const T y = lane < bs ? S.w[b0 + lane] : T(0);
@@ -725,46 +724,61 @@ __device__ __forceinline__ void cta_block_update(const T *__restrict__ M, int ld
     }
 }
 
-// Warp 0: lane r receives row b0 + r of the diagonal block (columns b0 .. b0 + bs),
-// loaded as coalesced row segments and transposed through a padded tile in S.P.
-template <class T>
-__device__ __forceinline__ void load_diag_rows(const T *__restrict__ A, int lda, int b0, int bs, T (&d)[32],
-                                               CtaSmem<T> &S) {
-    const int lane = threadIdx.x & 31;
-    T v[32];
-#pragma unroll
-    for (int r = 0; r < 32; r++) v[r] = (r < bs && lane < bs) ? A[(long long)(b0 + r) * lda + b0 + lane] : T(0);
-#pragma unroll
-    for (int r = 0; r < 32; r++) S.P[r * 33 + lane] = v[r];
-    __syncwarp();
-#pragma unroll
-    for (int c = 0; c < 32; c++) d[c] = S.P[lane * 33 + c];
-    __syncwarp();
-}
-
 // 1 / d for the factor type's solves: FP32 multiplies by the reciprocal, FP64 divides.
 template <class T>
 __device__ __forceinline__ T solve_div(T v, T d, T inv) {
     return sizeof(T) == 8 ? v / d : v * inv;
 }
 
+// Warp 0: solves the bs x bs diagonal block at (b0, b0) in place on S.w[b0 ..]. The
+// block's rows are staged in S.P (row r at r * 33); FORWARD runs top-down, TRANS takes
+// the block's transpose (L^T), UNIT skips the diagonal. Returns 1 when a diagonal entry
+// is below tiny (uniform over the warp).
+template <class T, bool FORWARD, bool UNIT, bool TRANS>
+__device__ __noinline__ int diag_block_solve(const T *__restrict__ A, int lda, int b0, int bs, CtaSmem<T> &S, T tiny) {
+    const int lane = threadIdx.x & 31;
+    T *D = S.P;
+    {
+        T v[32];
+#pragma unroll
+        for (int r = 0; r < 32; r++) v[r] = (r < bs && lane < bs) ? A[(long long)(b0 + r) * lda + b0 + lane] : T(0);
+#pragma unroll
+        for (int r = 0; r < 32; r++) D[r * 33 + lane] = v[r];
+    }
+    __syncwarp();
+    // lane's equation row: element (lane, c) of the block (or of its transpose)
+    auto elem = [&](int c) { return TRANS ? D[c * 33 + lane] : D[lane * 33 + c]; };
+    const T d = UNIT ? T(1) : elem(lane);
+    const int bad = UNIT ? 0 : __any_sync(0xffffffffu, lane < bs && absT(d) < tiny);
+    const T inv = T(1) / d;
+    T wv = lane < bs ? S.w[b0 + lane] : T(0);
+    if (FORWARD) {
+#pragma unroll 4
+        for (int jj = 0; jj < bs; jj++) {
+            if (!UNIT && lane == jj) wv = solve_div(wv, d, inv);
+            const T wj = __shfl_sync(0xffffffffu, wv, jj);
+            if (lane > jj) wv = fma(-elem(jj), wj, wv);
+        }
+    } else {
+#pragma unroll 4
+        for (int jj = bs - 1; jj >= 0; jj--) {
+            if (!UNIT && lane == jj) wv = solve_div(wv, d, inv);
+            const T wj = __shfl_sync(0xffffffffu, wv, jj);
+            if (lane < jj) wv = fma(-elem(jj), wj, wv);
+        }
+    }
+    if (lane < bs) S.w[b0 + lane] = wv;
+    __syncwarp();
+    return bad;
+}
+
 // Unit lower triangular solve L y = w (L strictly below the diagonal of A).
 template <class T>
 __device__ void cta_unit_lower_solve(const T *__restrict__ A, int lda, int n, CtaSmem<T> &S) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int warp = threadIdx.x >> 5;
     for (int b0 = 0; b0 < n; b0 += 32) {
         const int bs = min(32, n - b0);
-        if (warp == 0) {
-            T lr[32];
-            load_diag_rows(A, lda, b0, bs, lr, S);
-            T wv = lane < bs ? S.w[b0 + lane] : T(0);
-#pragma unroll
-            for (int jj = 0; jj < 31; jj++) {
-                const T wj = __shfl_sync(0xffffffffu, wv, jj);
-                if (lane > jj) wv = fma(-lr[jj], wj, wv);
-            }
-            if (lane < bs) S.w[b0 + lane] = wv;
-        }
+        if (warp == 0) diag_block_solve<T, true, true, false>(A, lda, b0, bs, S, T(0));
         __syncthreads();
         cta_block_update(A + b0, lda, b0 + bs, n, b0, bs, S);
         __syncthreads();
@@ -779,23 +793,7 @@ __device__ int cta_upper_solve(const T *__restrict__ A, int lda, int n, CtaSmem<
     for (int b1 = n; b1 > 0; b1 -= 32) {
         const int b0 = max(0, b1 - 32), bs = b1 - b0;
         if (warp == 0) {
-            T ur[32];
-            load_diag_rows(A, lda, b0, bs, ur, S);
-            T d = T(1);
-#pragma unroll
-            for (int jj = 0; jj < 32; jj++)
-                if (jj == lane) d = ur[jj];
-            const int bad = __any_sync(0xffffffffu, lane < bs && absT(d) < tiny);
-            const T inv = T(1) / d;
-            T wv = lane < bs ? S.w[b0 + lane] : T(0);
-#pragma unroll
-            for (int jj = 31; jj >= 0; jj--) {
-                if (jj >= bs) continue;
-                if (lane == jj) wv = solve_div(wv, d, inv);
-                const T wj = __shfl_sync(0xffffffffu, wv, jj);
-                if (lane < jj) wv = fma(-ur[jj], wj, wv);
-            }
-            if (lane < bs) S.w[b0 + lane] = wv;
+            const int bad = diag_block_solve<T, false, false, false>(A, lda, b0, bs, S, tiny);
             if (lane == 0) S.status = bad;
         }
         __syncthreads();
@@ -816,23 +814,7 @@ __device__ int cta_lower_solve(const T *__restrict__ A, int lda, int n, CtaSmem<
     for (int b0 = 0; b0 < n; b0 += 32) {
         const int bs = min(32, n - b0);
         if (warp == 0) {
-            T lr[32];
-            load_diag_rows(A, lda, b0, bs, lr, S);
-            T d = T(1);
-#pragma unroll
-            for (int jj = 0; jj < 32; jj++)
-                if (jj == lane) d = lr[jj];
-            const int bad = __any_sync(0xffffffffu, lane < bs && absT(d) < tiny);
-            const T inv = T(1) / d;
-            T wv = lane < bs ? S.w[b0 + lane] : T(0);
-#pragma unroll
-            for (int jj = 0; jj < 32; jj++) {
-                if (jj >= bs) break;
-                if (lane == jj) wv = solve_div(wv, d, inv);
-                const T wj = __shfl_sync(0xffffffffu, wv, jj);
-                if (lane > jj) wv = fma(-lr[jj], wj, wv);
-            }
-            if (lane < bs) S.w[b0 + lane] = wv;
+            const int bad = diag_block_solve<T, true, false, false>(A, lda, b0, bs, S, tiny);
             if (lane == 0) S.status = bad;
         }
         __syncthreads();
@@ -853,26 +835,7 @@ __device__ int cta_lower_t_solve(const T *__restrict__ A, int lda, int n, CtaSme
     for (int b1 = n; b1 > 0; b1 -= 32) {
         const int b0 = max(0, b1 - 32), bs = b1 - b0;
         if (warp == 0) {
-            // lane holds column `lane` of the block of L^T, i.e. L[b0 + jj][b0 + lane]
-            T lc[32];
-#pragma unroll
-            for (int jj = 0; jj < 32; jj++)
-                lc[jj] = (lane < bs && jj < bs && jj >= lane) ? A[(long long)(b0 + jj) * lda + b0 + lane] : T(0);
-            T d = T(1);
-#pragma unroll
-            for (int jj = 0; jj < 32; jj++)
-                if (jj == lane) d = lc[jj];
-            const int bad = __any_sync(0xffffffffu, lane < bs && absT(d) < tiny);
-            const T inv = T(1) / d;
-            T wv = lane < bs ? S.w[b0 + lane] : T(0);
-#pragma unroll
-            for (int jj = 31; jj >= 0; jj--) {
-                if (jj >= bs) continue;
-                if (lane == jj) wv = solve_div(wv, d, inv);
-                const T wj = __shfl_sync(0xffffffffu, wv, jj);
-                if (lane < jj) wv = fma(-lc[jj], wj, wv);
-            }
-            if (lane < bs) S.w[b0 + lane] = wv;
+            const int bad = diag_block_solve<T, false, false, true>(A, lda, b0, bs, S, tiny);
             if (lane == 0) S.status = bad;
         }
         __syncthreads();
@@ -949,7 +912,7 @@ __device__ int cta_factor_solve(const T *A, int lda, int n, int kind, CtaSmem<T>
 
 // Row-block passes over an n x n row-major matrix: a warp covers R consecutive rows x
 // 32 C columns per pass (lane owns columns lane + 32 c), every lane issuing its R C
-// loads before using any. (C, R) is picked from n (n <= 32 C) so that a lane keeps 16 to
+// loads before using any. (C, R) is picked from n (n <= 32 C) so that a lane keeps 8 to
 // 32 loads in flight.
 template <int C, int R, class TI, class TF>
 __device__ double copy_rows(const TI *__restrict__ A, int lda, int n, TF *__restrict__ W, int ldw) {
@@ -994,10 +957,8 @@ __device__ double cta_copy_convert(const TI *__restrict__ A, int lda, int n, TF 
         mx = copy_rows<8, 4>(A, lda, n, W, ldw);
     else if (n > 64)
         mx = copy_rows<4, 4>(A, lda, n, W, ldw);
-    else if (n > 32)
-        mx = copy_rows<2, 4>(A, lda, n, W, ldw);
     else
-        mx = copy_rows<1, 4>(A, lda, n, W, ldw);
+        mx = copy_rows<2, 4>(A, lda, n, W, ldw);
     return block_max(mx, S);
 }
 
@@ -1046,10 +1007,8 @@ __device__ double cta_residual(const TI *__restrict__ A, int lda, const TI *__re
         mx = residual_rows<8, 4>(A, lda, b, n, S);
     else if (n > 64)
         mx = residual_rows<4, 4>(A, lda, b, n, S);
-    else if (n > 32)
-        mx = residual_rows<2, 4>(A, lda, b, n, S);
     else
-        mx = residual_rows<1, 4>(A, lda, b, n, S);
+        mx = residual_rows<2, 4>(A, lda, b, n, S);
     return block_max(mx, S);
 }
 
