@@ -143,7 +143,7 @@ __device__ void batch_solve_one(const BatchDesc &d, int sys, const TI *__restric
 }
 
 template <class TI, class TF, bool MIXED>
-__global__ void __launch_bounds__(CTA_THREADS, 2) batch_solve_kernel(BatchDesc d, const TI *A, const TI *B, TI *X) {
+__global__ void __launch_bounds__(CTA_THREADS, CtaOcc<TF>::value) batch_solve_kernel(BatchDesc d, const TI *A, const TI *B, TI *X) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CtaSmem<TF> &S = *reinterpret_cast<CtaSmem<TF> *>(smem_raw);
     TF *W = static_cast<TF *>(d.work) + (long long)blockIdx.x * d.work_stride;

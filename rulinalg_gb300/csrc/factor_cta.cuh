@@ -41,6 +41,19 @@ struct CtaNB<double> {
     static constexpr int value = 16;
 };
 
+// CTAs per SM the one-CTA-per-system kernels are compiled for (register cap 65536 /
+// (256 x value)); the FP32 workspace fits three in shared memory, the FP64 one two.
+template <class T>
+struct CtaOcc;
+template <>
+struct CtaOcc<float> {
+    static constexpr int value = 3;
+};
+template <>
+struct CtaOcc<double> {
+    static constexpr int value = 2;
+};
+
 // Shared-memory workspace of one CTA (dynamic shared memory).
 template <class T>
 struct CtaSmem {
@@ -66,6 +79,30 @@ struct CtaSmem {
     int status;
     int item;
 };
+
+// double -> float, round to nearest even, by integer operations: the FP64 unit (which
+// also runs the hardware conversion) is the scarce one on this part. Results in the
+// normal float range are composed from the bit fields (the rounding carry may run into
+// the exponent, up to infinity, as it should); zeros, subnormal results, infinities and
+// NaNs take the hardware conversion.
+__device__ __forceinline__ float f64_to_f32_rn(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const unsigned e = (hi >> 20) & 0x7FFu;
+    if (e - 897u > 253u) return __double2float_rn(x);  // float exponent outside [1, 254]
+    unsigned f = (hi & 0x80000000u) | (((hi & 0x7FFFFFFFu) - 0x38000000u) << 3) | (lo >> 29);
+    const unsigned rem = lo & 0x1FFFFFFFu;
+    f += (rem > 0x10000000u || (rem == 0x10000000u && (f & 1u))) ? 1u : 0u;
+    return __uint_as_float(f);
+}
+
+template <class TF, class TI>
+__device__ __forceinline__ TF convert_to(TI v) {
+    if constexpr (sizeof(TF) == 4 && sizeof(TI) == 8)
+        return f64_to_f32_rn(v);
+    else
+        return (TF)v;
+}
 
 __device__ __forceinline__ float absT(float v) { return fabsf(v); }
 __device__ __forceinline__ double absT(double v) { return fabs(v); }
@@ -934,7 +971,7 @@ __device__ double copy_rows(const TI *__restrict__ A, int lda, int n, TF *__rest
 #pragma unroll
             for (int c = 0; c < C; c++) {
                 const int j = lane + 32 * c;
-                const TF f = (TF)v[r][c];
+                const TF f = convert_to<TF>(v[r][c]);
                 if (i < n && j < n) W[(long long)i * ldw + j] = f;
                 s += absT(f);
             }
