@@ -402,20 +402,19 @@ __device__ int cta_lu_factor(T *__restrict__ A, int lda, int n, CtaSmem<T> &S, T
             for (int c = 0; c < NB; c++) row[k][c] = (q < mrows && c < kb) ? src[c] : T(0);
         }
         if (tid == 0) S.nmoved = 0;
-        // One barrier per column. Step j: the warps' argmax candidates for column j (and
-        // their rows) were published in the previous step; every thread combines them,
-        // then updates its own active rows with the pivot row and forms its candidate for
-        // column j + 1, which its warp publishes for the next step.
+        // One barrier per column, the column loop rolled: every row is kept rotated so
+        // that row[k][0] holds the current column j. Step j combines the warps' argmax
+        // candidates for column j (published at the end of the previous step, rotated
+        // the same way), turns the active rows' row[k][0] into multipliers, updates
+        // their columns j + 1 .. NB - 1 (indices 1 .. NB - 1 - j) with the pivot row,
+        // and rotates every row left by one, the finished column-j entry going to the
+        // end. After NB steps the rows are back in column order.
         auto publish = [&](int j, int par) {
             T bv = T(-1);
             int bi = INT_MAX, bq = -1, bk = -1;
 #pragma unroll
             for (int k = 0; k < RPT; k++) {
-                T v = T(0);
-#pragma unroll
-                for (int c = 0; c < NB; c++)
-                    if (c == j) v = row[k][c];
-                const T av = absT(v);
+                const T av = absT(row[k][0]);
                 if (!used[k] && (av > bv || (av == bv && pos[k] < bi))) {
                     bv = av;
                     bi = pos[k];
@@ -443,12 +442,17 @@ __device__ int cta_lu_factor(T *__restrict__ A, int lda, int n, CtaSmem<T> &S, T
                 S.redq[par][warp] = wq;
             }
         };
-        publish(0, 0);
-        // Fully unrolled over the panel's columns: j is a compile-time constant in every
-        // copy, so the column selects and the c > j predicates cost nothing.
+        auto rotate = [&]() {
 #pragma unroll
-        for (int j = 0; j < NB; j++) {
-            if (j >= kb) break;
+            for (int k = 0; k < RPT; k++) {
+                const T first = row[k][0];
+#pragma unroll
+                for (int c = 0; c < NB - 1; c++) row[k][c] = row[k][c + 1];
+                row[k][NB - 1] = first;
+            }
+        };
+        publish(0, 0);
+        for (int j = 0; j < kb; j++) {
             const int par = j & 1;
             __syncthreads();
             T bv = S.redv[par][0];
@@ -468,11 +472,7 @@ __device__ int cta_lu_factor(T *__restrict__ A, int lda, int n, CtaSmem<T> &S, T
                 bi = j;
                 bq = -1;
                 bw = CTA_WARPS;
-                T d = S.cand[par][CTA_WARPS][0];
-#pragma unroll
-                for (int c = 0; c < NB; c++)
-                    if (c == j) d = S.cand[par][CTA_WARPS][c];
-                bv = absT(d);
+                bv = absT(S.cand[par][CTA_WARPS][0]);
             }
             if (bv < tiny) {
                 __syncthreads();
@@ -482,11 +482,9 @@ __device__ int cta_lu_factor(T *__restrict__ A, int lda, int n, CtaSmem<T> &S, T
             T prow[NB];
 #pragma unroll
             for (int c = 0; c < NB; c++) prow[c] = S.cand[par][bw][c];
-            T p = prow[0];
-#pragma unroll
-            for (int c = 0; c < NB; c++)
-                if (c == j) p = prow[c];
+            const T p = prow[0];
             const T inv_p = T(1) / p;  // one division per column; multipliers l = a_rj * (1/p)
+            const int act = NB - 1 - j;  // indices 1 .. act are the columns right of j
 #pragma unroll
             for (int k = 0; k < RPT; k++) {
                 const int q = tid + k * CTA_THREADS;
@@ -497,21 +495,19 @@ __device__ int cta_lu_factor(T *__restrict__ A, int lda, int n, CtaSmem<T> &S, T
                 } else if (pos[k] == j) {
                     pos[k] = bi;  // the row that held position j takes the pivot's old position
                 }
-                if (used[k]) continue;
-                T lj = row[k][0];
+                if (!used[k]) {
+                    // FP64 keeps gaussian_elimination's division (lu.rs:609); FP32 multiplies by 1/p
+                    const T l = sizeof(T) == 8 ? row[k][0] / p : row[k][0] * inv_p;
+                    row[k][0] = l;
 #pragma unroll
-                for (int c = 0; c < NB; c++)
-                    if (c == j) lj = row[k][c];
-                // FP64 keeps gaussian_elimination's division (lu.rs:609); FP32 multiplies by 1/p
-                const T l = sizeof(T) == 8 ? lj / p : lj * inv_p;
-#pragma unroll
-                for (int c = 0; c < NB; c++) {
-                    if (c > j) row[k][c] = fma(-l, prow[c], row[k][c]);
-                    if (c == j) row[k][c] = l;
+                    for (int c = 1; c < NB; c++)
+                        if (c <= act) row[k][c] = fma(-l, prow[c], row[k][c]);
                 }
             }
+            rotate();
             if (j + 1 < kb) publish(j + 1, par ^ 1);
         }
+        for (int j = kb; j < NB; j++) rotate();  // a narrow last panel: back to column order
         __syncthreads();
         // Rows to their final positions: shared panel (column-major, position order, for
         // the trailing update), global A, and the list of rows whose position changed.
@@ -647,10 +643,19 @@ __device__ int cta_chol_factor(T *__restrict__ A, int lda, int n, CtaSmem<T> &S,
             for (int c = 0; c < NB; c++) row[k][c] = (q < mrows && c < kb && c <= q) ? src[c] : T(0);
         }
         if (tid < kb) S.colj[0][tid] = row[0][0];
-        // Fully unrolled over the panel's columns (j is a compile-time constant per copy).
+        // The column loop is rolled, every row kept rotated so that row[k][0] holds the
+        // current column j (see cta_lu_factor); after NB steps the rows are back in
+        // column order.
+        auto rotate = [&]() {
 #pragma unroll
-        for (int j = 0; j < NB; j++) {
-            if (j >= kb) break;
+            for (int k = 0; k < RPT; k++) {
+                const T first = row[k][0];
+#pragma unroll
+                for (int c = 0; c < NB - 1; c++) row[k][c] = row[k][c + 1];
+                row[k][NB - 1] = first;
+            }
+        };
+        for (int j = 0; j < kb; j++) {
             const int par = j & 1;
             __syncthreads();
             const T d = S.colj[par][j];
@@ -660,32 +665,27 @@ __device__ int cta_chol_factor(T *__restrict__ A, int lda, int n, CtaSmem<T> &S,
             }
             const T s = sqrt(d);
             const T inv = T(1) / s;  // update factors; the stored entries keep the division
+            const int act = kb - 1 - j;  // indices 1 .. act are the panel columns right of j
             T lc[NB];
+            lc[0] = T(0);
 #pragma unroll
-            for (int c = 0; c < NB; c++) lc[c] = S.colj[par][c] * inv;
+            for (int c = 1; c < NB; c++) lc[c] = c <= act ? S.colj[par][j + c] * inv : T(0);
 #pragma unroll
             for (int k = 0; k < RPT; k++) {
                 const int q = tid + k * CTA_THREADS;
-                if (q < j || q >= mrows) continue;
-                T cr = row[k][0];
+                if (q >= j && q < mrows) {
+                    const T cr = row[k][0];
+                    const T l = cr / s, li = cr * inv;
+                    row[k][0] = l;
 #pragma unroll
-                for (int c = 0; c < NB; c++)
-                    if (c == j) cr = row[k][c];
-                const T l = cr / s, li = cr * inv;
-#pragma unroll
-                for (int c = 0; c < NB; c++) {
-                    if (c > j && c <= q && c < kb) row[k][c] = fma(-li, lc[c], row[k][c]);
-                    if (c == j) row[k][c] = l;
+                    for (int c = 1; c < NB; c++)
+                        if (c <= act && j + c <= q) row[k][c] = fma(-li, lc[c], row[k][c]);
                 }
             }
-            if (j + 1 < kb && tid < kb) {  // rows tid < kb are row[0] of threads 0..kb-1
-                T v = row[0][0];
-#pragma unroll
-                for (int c = 0; c < NB; c++)
-                    if (c == j + 1) v = row[0][c];
-                S.colj[par ^ 1][tid] = v;
-            }
+            rotate();
+            if (j + 1 < kb && tid < kb) S.colj[par ^ 1][tid] = row[0][0];  // rows tid < kb: row[0] of threads 0..kb-1
         }
+        for (int j = kb; j < NB; j++) rotate();  // a narrow last panel: back to column order
         // Write the factored panel: shared (column-major, for the SYRK) and global (the
         // lower part only; the strict upper triangle is never written).
 #pragma unroll
