@@ -50,10 +50,11 @@ def parse():
                    help="CPU baseline sample size in GFLOP of factorisation work")
     p.add_argument("--skip-e2e", action="store_true")
     p.add_argument("--skip-cpu", action="store_true")
-    p.add_argument("--workload", default="batch", choices=["batch", "dense", "mixed", "serve"],
+    p.add_argument("--workload", default="batch", choices=["batch", "dense", "mixed", "serve", "peaks"],
                    help="batch: the headline batched mix (default); dense: GEMM sweep n=1024..8192 f32/f64 "
                         "and plain FP64 LU; mixed: single-system mixed precision vs FP64 over n and kappa; "
-                        "serve: Poisson request stream through the serving loop")
+                        "serve: Poisson request stream through the serving loop; peaks: DFMA / FP64 mma / "
+                        "FFMA / host-copy probes (bench_peaks.cu)")
     p.add_argument("--sizes", default="", help="comma-separated sizes for dense / mixed")
     p.add_argument("--lambdas", default="1000,10000,50000", help="serve: arrival rates (requests/s)")
     return p.parse_args()
@@ -392,6 +393,28 @@ def serve_workload(args, rank, world, dev):
         print(json.dumps(line), flush=True)
 
 
+def peaks_workload(args, rank, world, dev):
+    """Builds and runs bench_peaks.cu (FP64 / FP32 pipe and host-copy probes)."""
+    import re
+    import tempfile
+    exe = Path(tempfile.mkdtemp()) / "bench_peaks"
+    subprocess.run(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
+                    str(ROOT / "bench_peaks.cu"), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+    vals = {}
+    for key, pat in (("dfma_tflops", r"DFMA\s+\S+ ms\s+(\S+) TFLOP"), ("ffma_tflops", r"FFMA\s+\S+ ms\s+(\S+) TFLOP"),
+                     ("dmma_m8n8k4_tflops", r"DMMA884\s+\S+ ms\s+(\S+) TFLOP"),
+                     ("dmma_m16n8k16_tflops", r"DMMA16816\s+\S+ ms\s+(\S+) TFLOP"),
+                     ("h2d_pinned_gbs", r"H2D pinned \S+ \S+ ms (\S+) GB"), ("d2h_pinned_gbs", r"D2H pinned \S+ \S+ ms (\S+) GB"),
+                     ("h2d_pageable_gbs", r"H2D pageable \S+ \S+ ms (\S+) GB")):
+        m = re.search(pat, out)
+        vals[key] = float(m.group(1)) if m else None
+    if rank == 0:
+        print(json.dumps({"metric": "FP64 DFMA peak", "value": vals["dfma_tflops"], "unit": "TFLOP/s", "n_gpus": world,
+                          "steps": 1, "warmup": 1, "higher_is_better": True, "data": "synthetic",
+                          "probes": vals, "raw": out.strip().splitlines()}), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -410,7 +433,8 @@ def main():
     torch.cuda.set_device(dev)
     if not rl.device_available():
         raise SystemExit("rulinalg_gb300: no usable sm_103 GPU")
-    other = {"dense": dense_workload, "mixed": mixed_workload, "serve": serve_workload}.get(args.workload)
+    other = {"dense": dense_workload, "mixed": mixed_workload, "serve": serve_workload,
+             "peaks": peaks_workload}.get(args.workload)
     if other is not None:
         other(args, rank, world, dev)
         if world > 1:

@@ -36,6 +36,13 @@ struct rl_batch_plan {
     void *h_a = nullptr, *h_b = nullptr, *h_x = nullptr;
     int *h_info = nullptr, *h_iters = nullptr;
     double *h_berr = nullptr;
+    // host-pointer pipeline: contiguous chunks of systems, each copied on its own stream
+    // while the previous chunk is solved (largest-first order within each chunk)
+    std::vector<int> chunk_first, chunk_count;
+    int *d_corder = nullptr, *d_ccounters = nullptr;
+    cudaStream_t copy = nullptr;
+    cudaEvent_t ev_start = nullptr;
+    std::vector<cudaEvent_t> ev_chunk;
 
     std::mutex mu;
 };
@@ -122,6 +129,46 @@ rl_status run_plan(rl_batch_plan *p, const TI *a, const TI *b, TI *x, int *info,
     return RL_OK;
 }
 
+template <class TI, class TF, bool MIXED>
+rl_status launch_chunk(rl_batch_plan *p, int c, const TI *a, const TI *b, TI *x, cudaStream_t s) {
+    const int first = p->chunk_first[c], cnt = p->chunk_count[c];
+    int *ctr = p->d_ccounters + 4 * c;
+    BatchDesc d{};
+    d.count = cnt;
+    d.count_dev = nullptr;
+    d.order = p->d_corder + first;
+    d.n = p->d_n;
+    d.kind = p->d_kind;
+    d.a_off = p->d_aoff;
+    d.b_off = p->d_boff;
+    d.next = ctr;
+    d.fb_list = p->d_fb_list + first;
+    d.fb_count = ctr + 1;
+    d.work = p->d_work;
+    d.work_stride = p->work_stride;
+    d.info = p->h_info;
+    d.iters = p->h_iters;
+    d.berr = p->h_berr;
+    d.iters_tag = 0;
+    d.max_iters = 30;
+    RL_LAUNCH((batch_solve_kernel<TI, TF, MIXED>), std::min(p->grid, cnt), CTA_THREADS, p->smem, s, d, a, b, x);
+    if (MIXED) {
+        BatchDesc f = d;
+        f.count = 0;
+        f.count_dev = ctr + 1;
+        f.order = d.fb_list;
+        f.next = ctr + 2;
+        f.work = p->d_work64;
+        f.iters_tag = -1;
+        RL_LAUNCH((batch_solve_kernel<TI, double, false>), std::min(p->grid64, cnt), CTA_THREADS, p->smem64, s, f, a,
+                  b, x);
+    }
+    return RL_OK;
+}
+
+// Host buffers in, host buffers out. The systems go in contiguous chunks: chunk c's
+// matrices and vectors are copied on the plan's copy stream while chunk c - 1 is solved
+// on the caller's stream, so the transfer and the solve overlap.
 template <class TI>
 rl_status solve_host(rl_batch_plan *p, const TI *a, const TI *b, TI *x, int32_t *info, int32_t *iters,
                      double *berr) {
@@ -133,21 +180,35 @@ rl_status solve_host(rl_batch_plan *p, const TI *a, const TI *b, TI *x, int32_t 
         RL_TRY_CUDA(cudaMalloc(&p->h_info, std::max<size_t>(1, p->count) * sizeof(int)));
         RL_TRY_CUDA(cudaMalloc(&p->h_iters, std::max<size_t>(1, p->count) * sizeof(int)));
         RL_TRY_CUDA(cudaMalloc(&p->h_berr, std::max<size_t>(1, p->count) * sizeof(double)));
+        RL_TRY_CUDA(cudaStreamCreateWithFlags(&p->copy, cudaStreamNonBlocking));
+        RL_TRY_CUDA(cudaEventCreateWithFlags(&p->ev_start, cudaEventDisableTiming));
+        p->ev_chunk.assign(p->chunk_first.size(), nullptr);
+        for (auto &e : p->ev_chunk) RL_TRY_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
     TI *da = static_cast<TI *>(p->h_a), *db = static_cast<TI *>(p->h_b), *dx = static_cast<TI *>(p->h_x);
-    if (p->a_total) RL_TRY_CUDA(cudaMemcpyAsync(da, a, p->a_total * sizeof(TI), cudaMemcpyHostToDevice, s));
-    if (p->b_total) RL_TRY_CUDA(cudaMemcpyAsync(db, b, p->b_total * sizeof(TI), cudaMemcpyHostToDevice, s));
-    rl_status st;
-    if (std::is_same<TI, float>::value)
-        st = run_plan<float, float, false>(p, (const float *)da, (const float *)db, (float *)dx, p->h_info,
-                                           p->h_iters, p->h_berr, s);
-    else if (p->precision == RL_PREC_MIXED)
-        st = run_plan<double, float, true>(p, (const double *)da, (const double *)db, (double *)dx, p->h_info,
-                                           p->h_iters, p->h_berr, s);
-    else
-        st = run_plan<double, double, false>(p, (const double *)da, (const double *)db, (double *)dx, p->h_info,
-                                             p->h_iters, p->h_berr, s);
-    RL_TRY(st);
+    const int nch = (int)p->chunk_first.size();
+    RL_TRY_CUDA(cudaMemsetAsync(p->d_ccounters, 0, 4 * std::max(1, nch) * sizeof(int), s));
+    RL_TRY_CUDA(cudaEventRecord(p->ev_start, s));  // earlier work on the buffers comes first
+    RL_TRY_CUDA(cudaStreamWaitEvent(p->copy, p->ev_start, 0));
+    for (int c = 0; c < nch; c++) {
+        const int first = p->chunk_first[c], end = first + p->chunk_count[c];
+        const long long a0 = p->a_off[first], a1 = end < (int)p->count ? p->a_off[end] : p->a_total;
+        const long long b0 = p->b_off[first], b1 = end < (int)p->count ? p->b_off[end] : p->b_total;
+        if (a1 > a0)
+            RL_TRY_CUDA(cudaMemcpyAsync(da + a0, a + a0, (a1 - a0) * sizeof(TI), cudaMemcpyHostToDevice, p->copy));
+        if (b1 > b0)
+            RL_TRY_CUDA(cudaMemcpyAsync(db + b0, b + b0, (b1 - b0) * sizeof(TI), cudaMemcpyHostToDevice, p->copy));
+        RL_TRY_CUDA(cudaEventRecord(p->ev_chunk[c], p->copy));
+        RL_TRY_CUDA(cudaStreamWaitEvent(s, p->ev_chunk[c], 0));
+        rl_status st;
+        if (std::is_same<TI, float>::value)
+            st = launch_chunk<float, float, false>(p, c, (const float *)da, (const float *)db, (float *)dx, s);
+        else if (p->precision == RL_PREC_MIXED)
+            st = launch_chunk<double, float, true>(p, c, (const double *)da, (const double *)db, (double *)dx, s);
+        else
+            st = launch_chunk<double, double, false>(p, c, (const double *)da, (const double *)db, (double *)dx, s);
+        RL_TRY(st);
+    }
     if (p->b_total) RL_TRY_CUDA(cudaMemcpyAsync(x, dx, p->b_total * sizeof(TI), cudaMemcpyDeviceToHost, s));
     if (info && p->count) RL_TRY_CUDA(cudaMemcpyAsync(info, p->h_info, p->count * sizeof(int), cudaMemcpyDeviceToHost, s));
     if (iters && p->count)
@@ -200,6 +261,28 @@ rl_status plan_init(rl_batch_plan *p, size_t count, const int32_t *n, const uint
     RL_TRY(upload(p->d_aoff, p->a_off, s));
     RL_TRY(upload(p->d_boff, p->b_off, s));
     RL_TRY(upload(p->d_order, order, s));
+    // Host-path chunks: up to 8 contiguous ranges of about equal matrix bytes, each with
+    // its own largest-first order.
+    {
+        const int want = (int)std::min<size_t>(8, std::max<size_t>(1, count));
+        std::vector<int> corder;
+        corder.reserve(count);
+        size_t i = 0;
+        for (int c = 0; c < want && i < count; c++) {
+            const long long target = (long long)((double)p->a_total * (c + 1) / want);
+            size_t e = i + 1;
+            while (e < count && (c == want - 1 || p->a_off[e] < target)) e++;
+            p->chunk_first.push_back((int)i);
+            p->chunk_count.push_back((int)(e - i));
+            std::vector<int> part;
+            for (int k : order)
+                if ((size_t)k >= i && (size_t)k < e) part.push_back(k);
+            corder.insert(corder.end(), part.begin(), part.end());
+            i = e;
+        }
+        RL_TRY(upload(p->d_corder, corder, s));
+        RL_TRY_CUDA(cudaMalloc(&p->d_ccounters, 4 * std::max<size_t>(1, p->chunk_first.size()) * sizeof(int)));
+    }
     RL_TRY_CUDA(cudaMalloc(&p->d_counters, 4 * sizeof(int)));
     RL_TRY_CUDA(cudaMalloc(&p->d_fb_list, std::max<size_t>(1, count) * sizeof(int)));
     const long long npad = (p->max_n + 3) & ~3;  // slot row stride rounded up to 4
@@ -230,8 +313,13 @@ rl_status plan_init(rl_batch_plan *p, size_t count, const int32_t *n, const uint
 void plan_free(rl_batch_plan *p) {
     if (p->exec) cudaGraphExecDestroy(p->exec);
     if (p->cap) cudaStreamDestroy(p->cap);
+    if (p->copy) cudaStreamDestroy(p->copy);
+    if (p->ev_start) cudaEventDestroy(p->ev_start);
+    for (cudaEvent_t e : p->ev_chunk)
+        if (e) cudaEventDestroy(e);
     void *ptrs[] = {p->d_n, p->d_order, p->d_counters, p->d_fb_list, p->d_kind, p->d_aoff, p->d_boff, p->d_work,
-                    p->d_work64, p->h_a, p->h_b, p->h_x, p->h_info, p->h_iters, p->h_berr};
+                    p->d_work64, p->h_a, p->h_b, p->h_x, p->h_info, p->h_iters, p->h_berr, p->d_corder,
+                    p->d_ccounters};
     for (void *q : ptrs)
         if (q) cudaFree(q);
 }

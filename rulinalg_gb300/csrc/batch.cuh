@@ -35,7 +35,7 @@ template <class TI, class TF>
 __device__ void store_solution(const BatchDesc &d, int sys, int n, TI *xi, CtaSmem<TF> &S, int st, int iters,
                                double berr) {
     if (st == RL_OK)
-        for (int i = threadIdx.x; i < n; i += CTA_THREADS) xi[i] = (TI)S.x[i];
+        for (int i = threadIdx.x; i < n; i += CTA_THREADS) xi[i] = (TI)S.x()[i];
     if (threadIdx.x == 0) {
         d.info[sys] = st;
         if (d.iters) d.iters[sys] = iters;
@@ -91,13 +91,13 @@ __device__ void batch_solve_one(const BatchDesc &d, int sys, const TI *__restric
         __syncthreads();
         return;
     }
-    for (int i = tid; i < n; i += CTA_THREADS) S.x[i] = (double)S.w[i];
+    for (int i = tid; i < n; i += CTA_THREADS) S.x()[i] = (double)S.w[i];
     __syncthreads();
 
     if (!MIXED) {
         const double rn = cta_residual<TI, TF>(Ai, n, bi, n, S);
         double xm = 0.0;
-        for (int i = tid; i < n; i += CTA_THREADS) xm = fmax(xm, fabs(S.x[i]));
+        for (int i = tid; i < n; i += CTA_THREADS) xm = fmax(xm, fabs(S.x()[i]));
         const double xn = block_max(xm, S);
         const double den = anorm * xn + bnorm;
         store_solution<TI, TF>(d, sys, n, xi, S, RL_OK, d.iters_tag, den > 0 ? rn / den : 0.0);
@@ -114,7 +114,7 @@ __device__ void batch_solve_one(const BatchDesc &d, int sys, const TI *__restric
     for (;; it++) {
         rn = cta_residual<TI, TF>(Ai, n, bi, n, S);
         double xm = 0.0;
-        for (int i = tid; i < n; i += CTA_THREADS) xm = fmax(xm, fabs(S.x[i]));
+        for (int i = tid; i < n; i += CTA_THREADS) xm = fmax(xm, fabs(S.x()[i]));
         xn = block_max(xm, S);
         if (rn <= stop * anorm * xn) {
             ok = true;
@@ -127,10 +127,10 @@ __device__ void batch_solve_one(const BatchDesc &d, int sys, const TI *__restric
         }
         prev = rn;
         const double scale = 1.0 / rn;
-        for (int i = tid; i < n; i += CTA_THREADS) S.w[i] = (TF)(S.r[i] * scale);
+        for (int i = tid; i < n; i += CTA_THREADS) S.w[i] = (TF)(S.r()[i] * scale);
         __syncthreads();
         if (cta_factor_solve<TF>(W, ldw, n, kind, S, tiny) != RL_OK) break;
-        for (int i = tid; i < n; i += CTA_THREADS) S.x[i] = fma(rn, (double)S.w[i], S.x[i]);
+        for (int i = tid; i < n; i += CTA_THREADS) S.x()[i] = fma(rn, (double)S.w[i], S.x()[i]);
         __syncthreads();
     }
     if (ok) {

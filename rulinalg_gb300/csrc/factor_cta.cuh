@@ -42,7 +42,8 @@ struct CtaNB<double> {
 };
 
 // CTAs per SM the one-CTA-per-system kernels are compiled for (register cap 65536 /
-// (256 x value)); the FP32 workspace fits three in shared memory, the FP64 one two.
+// (256 x value)); the FP32 workspace fits three in shared memory (four measured
+// slower under the 64-register cap), the FP64 one two.
 template <class T>
 struct CtaOcc;
 template <>
@@ -59,11 +60,12 @@ template <class T>
 struct CtaSmem {
     static constexpr int NB = CtaNB<T>::value;
     T P[NB * CTA_LDP];     // panel, column-major: P[c * CTA_LDP + r]
-    T Bt[NB * 128];        // one 128-column slice of U12
+    union {
+        T Bt[NB * 128];            // factorisation: one 128-column slice of U12, row-swap staging
+        double xr[2 * CTA_NMAX];   // refinement (after the factorisation): FP64 x, then FP64 r
+    } u;
     T Linv[NB * (NB + 1)]; // L11^-1 of the current LU panel
     T w[CTA_NMAX];         // factor-precision right-hand side / solution
-    double x[CTA_NMAX];    // FP64 solution (refinement)
-    double r[CTA_NMAX];    // FP64 residual
     int piv[CTA_NMAX];     // LAPACK-style pivots: step j swapped rows j and piv[j]
     int rowperm[CTA_NMAX]; // the same as a position -> original row map (solves)
     T cand[2][CTA_WARPS + 1][NB];  // per-warp pivot candidate rows (+ the position-j row),
@@ -78,6 +80,8 @@ struct CtaSmem {
     int redq[2][CTA_WARPS];  // panel row of the warp's candidate
     int status;
     int item;
+    __device__ double *x() { return u.xr; }             // FP64 solution (refinement)
+    __device__ double *r() { return u.xr + CTA_NMAX; }  // FP64 residual
 };
 
 // double -> float, round to nearest even, by integer operations: the FP64 unit (which
@@ -535,7 +539,7 @@ __device__ int cta_lu_factor(T *__restrict__ A, int lda, int n, CtaSmem<T> &S, T
         // flight), then written to their destinations.
         {
             const int nmv = S.nmoved;
-            T *stage = S.Bt;  // NB * 64 >= 2 NB rows x 32 columns
+            T *stage = S.u.Bt;  // NB * 64 >= 2 NB rows x 32 columns
             constexpr int CW = 32;
             for (int c0 = 0; c0 < n - kb && nmv > 0; c0 += CW) {
                 constexpr int K = (2 * NB * CW) / CTA_THREADS;
@@ -586,7 +590,7 @@ __device__ int cta_lu_factor(T *__restrict__ A, int lda, int n, CtaSmem<T> &S, T
                     v[k] = (tj + cc < n2) ? A[(long long)(k0 + pp) * lda + k0 + kb + tj + cc] : T(0);
                 }
 #pragma unroll
-                for (int k = 0; k < K; k++) S.Bt[tid + k * CTA_THREADS] = v[k];
+                for (int k = 0; k < K; k++) S.u.Bt[tid + k * CTA_THREADS] = v[k];
             }
             __syncthreads();
             {
@@ -596,14 +600,14 @@ __device__ int cta_lu_factor(T *__restrict__ A, int lda, int n, CtaSmem<T> &S, T
                 for (int i = 0; i < RPS; i++) u[i] = T(0);
 #pragma unroll
                 for (int k = 0; k < NB; k++) {
-                    const T bk = S.Bt[k * 128 + cc];
+                    const T bk = S.u.Bt[k * 128 + cc];
 #pragma unroll
                     for (int i = 0; i < RPS; i++) u[i] = fma(S.Linv[(rg + i) * (NB + 1) + k], bk, u[i]);
                 }
                 __syncthreads();
 #pragma unroll
                 for (int i = 0; i < RPS; i++) {
-                    S.Bt[(rg + i) * 128 + cc] = u[i];
+                    S.u.Bt[(rg + i) * 128 + cc] = u[i];
                     if (tj + cc < n2) A[(long long)(k0 + rg + i) * lda + k0 + kb + tj + cc] = u[i];
                 }
             }
@@ -611,7 +615,7 @@ __device__ int cta_lu_factor(T *__restrict__ A, int lda, int n, CtaSmem<T> &S, T
             constexpr int TS = TileCfg<T>::TS;
             for (int ti = 0; ti < m2; ti += TS)
                 for (int tc = 0; tc < 128 && tj + tc < n2; tc += TS)
-                    update_tile<T, NB>(A, lda, k0, mrows, kb + ti, kb + tj + tc, S.P, S.Bt, 128, tc, vec,
+                    update_tile<T, NB>(A, lda, k0, mrows, kb + ti, kb + tj + tc, S.P, S.u.Bt, 128, tc, vec,
                                        [&](int, int c) { return kb + n2 - c; });
             __syncthreads();
         }
@@ -915,8 +919,7 @@ __device__ void cta_build_rowperm(int n, CtaSmem<T> &S) {
     __syncthreads();
 }
 
-// Applies the row permutation to S.w as a gather (through S.x's storage as scratch when
-// T is float; a second pass otherwise).
+// Applies the row permutation to S.w as a gather through registers.
 template <class T>
 __device__ void cta_apply_pivots(int n, CtaSmem<T> &S) {
     T v[CTA_NMAX / CTA_THREADS];
@@ -987,15 +990,16 @@ __device__ double copy_rows(const TI *__restrict__ A, int lda, int n, TF *__rest
 template <class TI, class TF>
 __device__ double cta_copy_convert(const TI *__restrict__ A, int lda, int n, TF *__restrict__ W, int ldw,
                                    CtaSmem<TF> &S) {
+    constexpr int H = CtaOcc<TF>::value >= 4 ? 2 : 1;  // fewer loads in flight under a 64-register cap
     double mx;
     if (n > 256)
-        mx = copy_rows<16, 2>(A, lda, n, W, ldw);
+        mx = copy_rows<16, 2 / H>(A, lda, n, W, ldw);
     else if (n > 128)
-        mx = copy_rows<8, 4>(A, lda, n, W, ldw);
+        mx = copy_rows<8, 4 / H>(A, lda, n, W, ldw);
     else if (n > 64)
-        mx = copy_rows<4, 4>(A, lda, n, W, ldw);
+        mx = copy_rows<4, 4 / H>(A, lda, n, W, ldw);
     else
-        mx = copy_rows<2, 4>(A, lda, n, W, ldw);
+        mx = copy_rows<2, 4 / H>(A, lda, n, W, ldw);
     return block_max(mx, S);
 }
 
@@ -1019,12 +1023,12 @@ __device__ double residual_rows(const TI *__restrict__ A, int lda, const TI *__r
 #pragma unroll
             for (int c = 0; c < C; c++) {
                 const int j = lane + 32 * c;
-                s = fma((double)v[r][c], j < n ? S.x[j] : 0.0, s);
+                s = fma((double)v[r][c], j < n ? S.x()[j] : 0.0, s);
             }
             s = warp_sum(s);
             const double ri = __shfl_sync(0xffffffffu, bl, r) - s;
             if (i0 + r < n) {
-                if (lane == 0) S.r[i0 + r] = ri;
+                if (lane == 0) S.r()[i0 + r] = ri;
                 mx = fmax(mx, fabs(ri));
             }
         }
@@ -1037,15 +1041,16 @@ __device__ double residual_rows(const TI *__restrict__ A, int lda, const TI *__r
 // order, then the warp tree adds the lanes.
 template <class TI, class T>
 __device__ double cta_residual(const TI *__restrict__ A, int lda, const TI *__restrict__ b, int n, CtaSmem<T> &S) {
+    constexpr int H = CtaOcc<T>::value >= 4 ? 2 : 1;
     double mx;
     if (n > 256)
-        mx = residual_rows<16, 2>(A, lda, b, n, S);
+        mx = residual_rows<16, 2 / H>(A, lda, b, n, S);
     else if (n > 128)
-        mx = residual_rows<8, 4>(A, lda, b, n, S);
+        mx = residual_rows<8, 4 / H>(A, lda, b, n, S);
     else if (n > 64)
-        mx = residual_rows<4, 4>(A, lda, b, n, S);
+        mx = residual_rows<4, 4 / H>(A, lda, b, n, S);
     else
-        mx = residual_rows<2, 4>(A, lda, b, n, S);
+        mx = residual_rows<2, 4 / H>(A, lda, b, n, S);
     return block_max(mx, S);
 }
 
