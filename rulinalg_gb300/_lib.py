@@ -80,6 +80,8 @@ SIGNATURES = {
     "rl_dsolve_mixed_dev": (st, [sz, sz, C.c_int, vp, sz, vp, sz, vp, sz, vp, vp]),
     "rl_dsolve_mixed": (st, [sz, sz, C.c_int, f64p, sz, f64p, sz, f64p, sz, vp]),
     "rl_dsolve_fp64_dev": (st, [sz, sz, C.c_int, vp, sz, vp, sz, vp, sz, vp, vp]),
+    "rl_dlstsq_mixed_dev": (st, [sz, sz, vp, sz, vp, vp, vp, vp]),
+    "rl_dlstsq_mixed": (st, [sz, sz, f64p, sz, f64p, f64p, vp]),
     "rl_server_create": (st, [vp, C.POINTER(vp)]),
     "rl_server_submit": (st, [vp, vp, C.POINTER(C.c_uint64)]),
     "rl_server_wait": (st, [vp, C.c_uint64, C.c_double, vp]),

@@ -372,3 +372,22 @@ def solve_mixed(matrix, b, kind: str = "lu"):
     out = {"iters": info.iters, "gmres_iters": info.gmres_iters, "path": PATHS.get(info.path, info.path),
            "berr": info.berr}
     return (x[:, 0] if vec else x), out
+
+
+def lstsq_mixed(matrix, b):
+    """min ||A x - b||_2 (m >= n) through the mixed-precision least-squares solver (FP32
+    Householder QR, FP64 corrected semi-normal-equation refinement, FP64 QR fallback).
+    Returns (x, info) with iters, path and berr (the scaled normal-equations residual)."""
+    from ._lib import SolveInfo
+    a = np.ascontiguousarray(matrix, dtype=np.float64)
+    if a.ndim != 2:
+        raise RulinalgPanic("Matrix must be two-dimensional.")
+    m, n = a.shape
+    bb = np.ascontiguousarray(b, dtype=np.float64).reshape(-1)
+    if bb.shape[0] != m:
+        raise RulinalgPanic("Matrix and vector dimensions are not compatible.")
+    x = np.zeros(n, dtype=np.float64)
+    info = SolveInfo()
+    _check(lib.rl_dlstsq_mixed(m, n, _ptr(a), max(n, 1), _ptr(bb), _ptr(x), C.byref(info)))
+    return x, {"iters": info.iters, "gmres_iters": info.gmres_iters, "path": PATHS.get(info.path, info.path),
+               "berr": info.berr}

@@ -90,11 +90,16 @@ static __global__ void __launch_bounds__(256) lu_panel_kernel(T *P, long long ld
     const int r0 = g * rows_per, r1 = min(mrows, r0 + rows_per), nr = max(0, r1 - r0);
     const int CS = 2 + NB;  // candidate record: |v|, row, then the row's values
 
+    // Identity pivots first: a launch that stops early (error or timeout) still leaves
+    // in-range pivots for the row swaps that follow it on the stream.
+    if (g == 0)
+        for (int j = tid; j < kb; j += blockDim.x) ipiv[j] = k0 + j;
     for (int idx = tid; idx < nr * kb; idx += blockDim.x) {
         const int r = idx / kb, c = idx - r * kb;
         R[r * LDR + c] = P[(long long)(r0 + r) * lda + c];
     }
     __syncthreads();
+    __shared__ int s_q[8];
     for (int j = 0; j < kb; j++) {
         const int slot = j & 1;
         T bv = T(-1);
@@ -123,20 +128,37 @@ static __global__ void __launch_bounds__(256) lu_panel_kernel(T *P, long long ld
         if (bi != INT_MAX && tid < kb) mine[2 + tid] = R[(bi - r0) * LDR + tid];
         if (j >= r0 && j < r1 && tid < kb) rowj[slot * NB + tid] = R[(j - r0) * LDR + tid];
         if (!grid_barrier(&sync->ctr, (unsigned)(G * (j + 1)), &sync->err)) return;
-        // Winner over all CTAs, identical in every CTA.
+        // Winner over all CTAs, identical in every CTA: thread q reads CTA q's candidate,
+        // then a block argmax (largest |v|, smallest row on ties).
         T wv = T(-1);
         int wi = INT_MAX, wg = -1;
-        for (int q = 0; q < G; q++) {
+        for (int q = tid; q < G; q += blockDim.x) {
             const volatile T *c = cand + ((size_t)slot * G + q) * CS;
             const T v = c[0];
             const int i = (int)c[1];
-            if (i < 0) continue;
-            if (v > wv || (v == wv && i < wi)) {
+            if (i >= 0 && (v > wv || (v == wv && i < wi))) {
                 wv = v;
                 wi = i;
                 wg = q;
             }
         }
+        warp_amax3(wv, wi, wg);
+        __syncthreads();  // s_v / s_i of the local argmax are read no more
+        if (lane == 0) {
+            s_v[warp] = wv;
+            s_i[warp] = wi;
+            s_q[warp] = wg;
+        }
+        __syncthreads();
+        wv = s_v[0];
+        wi = s_i[0];
+        wg = s_q[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++)
+            if (s_v[w] > wv || (s_v[w] == wv && s_i[w] < wi)) {
+                wv = s_v[w];
+                wi = s_i[w];
+                wg = s_q[w];
+            }
         if (wi == INT_MAX) {  // no finite candidate (NaN column): keep the diagonal
             wi = j;
             wg = -1;
@@ -219,8 +241,15 @@ static __global__ void __launch_bounds__(256) qr_panel_kernel(T *P, long long ld
             if (j >= r0 && j < r1) x0buf[slot] = R[(j - r0) * LDR + j];
         }
         if (!grid_barrier(&sync->ctr, (unsigned)(G * (++phase)), &sync->err)) return;
+        // sigma = sum of the CTAs' partials, a fixed tree over q (thread q, then warps)
         T sigma = T(0);
-        for (int q = 0; q < G; q++) sigma += ((volatile T *)part)[((size_t)slot * G + q) * PS];
+        for (int q = tid; q < G; q += blockDim.x) sigma += ((volatile T *)part)[((size_t)slot * G + q) * PS];
+        sigma = warp_sum(sigma);
+        __syncthreads();  // s_red from step (1) is read no more
+        if (lane == 0) s_red[warp][0] = sigma;
+        __syncthreads();
+        sigma = T(0);
+        for (int w = 0; w < nw; w++) sigma += s_red[w][0];
         const T x0 = ((volatile T *)x0buf)[slot];
         if (sigma == T(0)) {  // already a multiple of e1: tau = 0, nothing changes
             if (g == 0 && tid == 0) tau[j] = T(0);
@@ -244,10 +273,12 @@ static __global__ void __launch_bounds__(256) qr_panel_kernel(T *P, long long ld
             if (lane == 0) part[((size_t)slot * G + g) * PS + 1 + c] = acc;
         }
         if (!grid_barrier(&sync->ctr, (unsigned)(G * (++phase)), &sync->err)) return;
-        if (tid >= j && tid < kb) {
+        // u_c = sum over CTAs of the partials: warp per column, lanes over CTAs
+        for (int c = j + warp; c < kb; c += nw) {
             T a = T(0);
-            for (int q = 0; q < G; q++) a += ((volatile T *)part)[((size_t)slot * G + q) * PS + 1 + tid];
-            u[tid] = a;
+            for (int q = lane; q < G; q += 32) a += ((volatile T *)part)[((size_t)slot * G + q) * PS + 1 + c];
+            a = warp_sum(a);
+            if (lane == 0) u[c] = a;
         }
         __syncthreads();
         // (3) a[r][c] += (-tau v_r) u_c for c > j (ger, internal_utils.rs:67-83); the

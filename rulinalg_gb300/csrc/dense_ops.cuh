@@ -77,20 +77,20 @@ rl_status lu_factor_dev(T *A, long long lda, int n, int *ipiv, cudaStream_t s, T
     RL_TRY(set_smem(pk, 200 * 1024));
     const size_t tsm = sizeof(T) * (64 * 65 + 64 * 64);
     RL_TRY(set_smem(trsm_diag_kernel<T>, tsm));
+    // The error word is sticky across panels (only the barrier counter is reset per
+    // launch) and read once at the end: a failed panel leaves identity pivots, the work
+    // after it runs on in-range indices, and every later panel stops at its first barrier.
+    RL_TRY_CUDA(cudaMemsetAsync(sync.p, 0, sizeof(PanelSync), s));
     for (int k0 = 0; k0 < n; k0 += NB) {
         const int kb = std::min(NB, n - k0), mrows = n - k0;
         int G, rows_per;
         panel_geometry<T>(mrows, G, rows_per);
         const size_t smem = ((size_t)rows_per * (NB + 1) + NB) * sizeof(T);
-        RL_TRY_CUDA(cudaMemsetAsync(sync.p, 0, sizeof(PanelSync), s));
+        if (k0 > 0) RL_TRY_CUDA(cudaMemsetAsync(&sync.p->ctr, 0, sizeof(unsigned), s));
         T *P = A + (long long)k0 * lda + k0;
         int *ip = ipiv + k0;
         void *args[] = {&P, &lda, (void *)&mrows, (void *)&kb, &k0, &rows_per, &ip, &cand.p, &rowj.p, &sync.p, &tiny};
         RL_TRY(launch_coop<T>((void *)pk, G, smem, args, s));
-        int err = 0;
-        RL_TRY_CUDA(cudaMemcpyAsync(&err, &sync.p->err, sizeof(int), cudaMemcpyDeviceToHost, s));
-        RL_TRY_CUDA(cudaStreamSynchronize(s));
-        if (err) return err;
         const int nother = n - kb;
         if (nother > 0)
             RL_LAUNCH(laswp_kernel<T>, ceil_div(nother, 256), 256, 0, s, A, lda, n, k0, k0 + kb, ipiv, k0, k0 + kb);
@@ -104,7 +104,10 @@ rl_status lu_factor_dev(T *A, long long lda, int n, int *ipiv, cudaStream_t s, T
                                          P + (long long)kb * lda + kb, lda, s)));
         }
     }
-    return RL_OK;
+    int err = 0;
+    RL_TRY_CUDA(cudaMemcpyAsync(&err, &sync.p->err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    RL_TRY_CUDA(cudaStreamSynchronize(s));
+    return err;
 }
 
 // Blocked right-looking Cholesky: diagonal block by one CTA, L21 = A21 L11^-T, SYRK.
@@ -149,20 +152,18 @@ rl_status qr_factor_dev(T *A, long long lda, int m, int n, int nrefl, T *tau, cu
     RL_TRY(W2.alloc((size_t)NB * std::max(1, n), s));
     auto pk = qr_panel_kernel<T>;
     RL_TRY(set_smem(pk, 200 * 1024));
+    // Sticky error word, read once at the end (see lu_factor_dev).
+    RL_TRY_CUDA(cudaMemsetAsync(sync.p, 0, sizeof(PanelSync), s));
     for (int k0 = 0; k0 < nrefl; k0 += NB) {
         const int kb = std::min(NB, nrefl - k0), mrows = m - k0;
         int G, rows_per;
         panel_geometry<T>(mrows, G, rows_per);
         const size_t smem = ((size_t)rows_per * (NB + 1) + NB) * sizeof(T);
-        RL_TRY_CUDA(cudaMemsetAsync(sync.p, 0, sizeof(PanelSync), s));
+        if (k0 > 0) RL_TRY_CUDA(cudaMemsetAsync(&sync.p->ctr, 0, sizeof(unsigned), s));
         T *P = A + (long long)k0 * lda + k0;
         T *tk = tau + k0;
         void *args[] = {&P, &lda, (void *)&mrows, (void *)&kb, &rows_per, &tk, &part.p, &x0buf.p, &sync.p};
         RL_TRY(launch_coop<T>((void *)pk, G, smem, args, s));
-        int err = 0;
-        RL_TRY_CUDA(cudaMemcpyAsync(&err, &sync.p->err, sizeof(int), cudaMemcpyDeviceToHost, s));
-        RL_TRY_CUDA(cudaStreamSynchronize(s));
-        if (err) return err;
         const int n2 = n - k0 - kb;
         if (n2 <= 0) continue;
         const long long mk = (long long)mrows * kb;
@@ -174,7 +175,10 @@ rl_status qr_factor_dev(T *A, long long lda, int m, int n, int nrefl, T *tau, cu
         RL_TRY((gemm<T, true, false>(kb, n2, kb, T(1), Tm.p, kb, W1.p, n2, T(0), W2.p, n2, s)));
         RL_TRY((gemm<T, false, false>(mrows, n2, kb, T(-1), V.p, kb, W2.p, n2, T(1), A2, lda, s)));
     }
-    return RL_OK;
+    int err = 0;
+    RL_TRY_CUDA(cudaMemcpyAsync(&err, &sync.p->err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    RL_TRY_CUDA(cudaStreamSynchronize(s));
+    return err;
 }
 
 // Q[:, 0:k] of a compact QR (HouseholderComposition::first_k_columns): reflector panels

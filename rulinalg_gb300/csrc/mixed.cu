@@ -87,4 +87,43 @@ rl_status rl_dsolve_mixed(size_t n, size_t nrhs, int kind, const double *a, size
     return RL_OK;
 }
 
+rl_status rl_dlstsq_mixed_dev(size_t m, size_t n, const double *a, size_t lda, const double *b, double *x,
+                              rl_solve_info *info, void *stream) {
+    if (m < n) return RL_ERR_SHAPE;
+    if (n == 0) {
+        fill_info(info, SolveOut());
+        return RL_OK;
+    }
+    if (!a || !b || !x || lda < n || m > (size_t)INT32_MAX) return RL_ERR_INVALID_ARG;
+    RL_TRY(ensure_device());
+    SolveOut o;
+    RL_TRY(lstsq_mixed(a, (long long)lda, (int)m, (int)n, b, x, o, resolve_stream(stream)));
+    fill_info(info, o);
+    return RL_OK;
+}
+
+rl_status rl_dlstsq_mixed(size_t m, size_t n, const double *a, size_t lda, const double *b, double *x,
+                          rl_solve_info *info) {
+    if (m < n) return RL_ERR_SHAPE;
+    if (n == 0) {
+        fill_info(info, SolveOut());
+        return RL_OK;
+    }
+    if (!a || !b || !x || lda < n || m > (size_t)INT32_MAX) return RL_ERR_INVALID_ARG;
+    RL_TRY(ensure_device());
+    cudaStream_t s = cudaStreamPerThread;
+    DevBuf<double> dA, dB, dX;
+    RL_TRY(dA.alloc(m * n, s));
+    RL_TRY(dB.alloc(m, s));
+    RL_TRY(dX.alloc(n, s));
+    RL_TRY(copy_h2d(dA.p, n, a, lda, m, n, s));
+    RL_TRY_CUDA(cudaMemcpyAsync(dB.p, b, m * sizeof(double), cudaMemcpyHostToDevice, s));
+    SolveOut o;
+    RL_TRY(lstsq_mixed(dA.p, (long long)n, (int)m, (int)n, dB.p, dX.p, o, s));
+    RL_TRY_CUDA(cudaMemcpyAsync(x, dX.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    RL_TRY_CUDA(cudaStreamSynchronize(s));
+    fill_info(info, o);
+    return RL_OK;
+}
+
 }  // extern "C"

@@ -284,4 +284,88 @@ static __global__ void combine_kernel(double *__restrict__ x, const double *__re
     }
 }
 
+// ------------------------------------------------------- mixed-precision least squares --
+// A32 = (float)A for an m x n matrix (row strides lda / ld32) and ||A||_inf in FP64 into
+// *anorm_bits. Warp per row.
+static __global__ void to_f32_rect_kernel(const double *__restrict__ A, long long lda, int m, int n,
+                                          float *__restrict__ A32, long long ld32, unsigned long long *anorm_bits) {
+    const int lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    for (int i = blockIdx.x * wpb + (threadIdx.x >> 5); i < m; i += gridDim.x * wpb) {
+        const double *row = A + (long long)i * lda;
+        float *out = A32 + (long long)i * ld32;
+        double s = 0.0;
+        for (int j = lane; j < n; j += 32) {
+            const double v = row[j];
+            out[j] = (float)v;
+            s += fabs(v);
+        }
+        s = warp_sum(s);
+        if (lane == 0) atomic_max_nonneg(anorm_bits, s);
+    }
+}
+
+// r = b - A x for an m x n matrix and one right-hand side, FP64; warp per row.
+static __global__ void resid_rect_kernel(const double *__restrict__ A, long long lda, int m, int n,
+                                         const double *__restrict__ x, const double *__restrict__ b,
+                                         double *__restrict__ r) {
+    const int lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    for (int i = blockIdx.x * wpb + (threadIdx.x >> 5); i < m; i += gridDim.x * wpb) {
+        const double *row = A + (long long)i * lda;
+        double s0 = 0.0, s1 = 0.0;
+        int j = lane;
+        for (; j + 32 < n; j += 64) {
+            s0 = fma(row[j], x[j], s0);
+            s1 = fma(row[j + 32], x[j + 32], s1);
+        }
+        if (j < n) s0 = fma(row[j], x[j], s0);
+        const double sum = warp_sum(s0 + s1);
+        if (lane == 0) r[i] = b[i] - sum;
+    }
+}
+
+// partial[c * n + j] = sum over the rows i of chunk c (rows_per rows) of A[i][j] r[i]:
+// thread per column (coalesced rows), four independent accumulators.
+static __global__ void gemv_t_partial_kernel(const double *__restrict__ A, long long lda, int m, int n,
+                                             const double *__restrict__ r, int rows_per, double *__restrict__ partial) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int i0 = blockIdx.y * rows_per, i1 = min(m, i0 + rows_per);
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    int i = i0;
+    for (; i + 3 < i1; i += 4) {
+        a0 = fma(A[(long long)i * lda + j], r[i], a0);
+        a1 = fma(A[(long long)(i + 1) * lda + j], r[i + 1], a1);
+        a2 = fma(A[(long long)(i + 2) * lda + j], r[i + 2], a2);
+        a3 = fma(A[(long long)(i + 3) * lda + j], r[i + 3], a3);
+    }
+    for (; i < i1; i++) a0 = fma(A[(long long)i * lda + j], r[i], a0);
+    partial[(long long)blockIdx.y * n + j] = (a0 + a1) + (a2 + a3);
+}
+
+// g[j] = sum over chunks c (in order) of partial[c * n + j].
+static __global__ void reduce_chunks_kernel(const double *__restrict__ partial, int chunks, int n, double *__restrict__ g) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int c = 0; c < chunks; c++) s += partial[(long long)c * n + j];
+        g[j] = s;
+    }
+}
+
+// L = R^T (lower, row stride n) from the n x n upper triangle R at the top of a compact
+// QR (row stride ldq); the strict upper part of L is zero.
+static __global__ void upper_to_lower_t_kernel(const float *__restrict__ QR, long long ldq, int n, float *__restrict__ L) {
+    const long long total = (long long)n * n;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(e / n), j = (int)(e - (long long)i * n);
+        L[e] = j <= i ? QR[(long long)j * ldq + i] : 0.f;
+    }
+}
+
+// x += d
+static __global__ void add_kernel(double *__restrict__ x, const double *__restrict__ d, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] += d[i];
+}
+
 }  // namespace rl

@@ -101,7 +101,9 @@ struct Dots {
 // CGS2 orthogonalisation; Givens rotations and the small triangular solve on the GPU.
 inline rl_status gmres_ir(const double *A, long long lda, int n, const Minv &M, const double *b, double *x, double anorm,
                    double bnorm, SolveOut &out, bool &ok, cudaStream_t s) {
-    constexpr int m = 48, outer_max = 20;
+    // At most two restart cycles, and the second only if the first cut the residual
+    // tenfold: past that an FP64 refactorisation is the cheaper way to the answer.
+    constexpr int m = 48, outer_max = 3;
     const double inner_tol = 1e-8;
     DevBuf<double> V, H, cs, sn, g, y, w, r, t, nrm2, partial;
     DevBuf<unsigned long long> bits;
@@ -121,6 +123,7 @@ inline rl_status gmres_ir(const double *A, long long lda, int n, const Minv &M, 
     Dots dots{partial.p, P};
     const int gv = std::min(4 * num_sms(), ceil_div(n, 256));
     ok = false;
+    double prev_rn = INFINITY;
     for (int outer = 0; outer < outer_max; outer++) {
         RL_TRY(residual_dev(A, lda, n, x, 1, b, 1, r.p, 1, 1, s));
         RL_TRY(colnorm_dev(r.p, 1, n, 1, bits.p, s));
@@ -135,6 +138,8 @@ inline rl_status gmres_ir(const double *A, long long lda, int n, const Minv &M, 
             ok = true;
             return RL_OK;
         }
+        if (outer == outer_max - 1 || !(rn <= 0.1 * prev_rn)) return RL_OK;  // out of budget, or no progress
+        prev_rn = rn;
         // z = M^-1 r -> V[0] = z / ||z||, g = (||z||, 0, ...)
         RL_TRY(M.apply(r.p, w.p, s));
         RL_TRY(dots.run(w.p, 0, 1, w.p, n, nrm2.p, 0, s));
@@ -369,7 +374,7 @@ struct MixedFactor {
         RL_TRY_CUDA(cudaMemset2DAsync(X, ldx * sizeof(double), 0, nrhs * sizeof(double), n, s));
         RL_LAUNCH(update_x_kernel, ge, 256, 0, s, X, ldx, W.p, (long long)nrhs, n, nrhs, bn_b, active.p);
         std::vector<unsigned long long> hb(3 * nrhs);
-        bool stalled = false, need_fp64 = false;
+        bool stalled = false, need_fp64 = false, diverged = false;
         for (int it = 0;; it++) {
             RL_TRY(residual_dev(A, lda, n, X, ldx, B, ldb, R.p, nrhs, nrhs, s));
             RL_TRY(colnorm_dev(R.p, nrhs, n, nrhs, rn_b, s));
@@ -392,6 +397,9 @@ struct MixedFactor {
                 berr = std::max(berr, den > 0 ? rn / den : 0.0);
                 // diverging (a growing residual) or stalling (not halving after two steps)
                 if (!conv[c] && ((it >= 1 && rn > prev[c]) || (it >= 2 && rn > 0.5 * prev[c]))) stalled = true;
+                // the first correction made things worse: the FP32 factor is too far off
+                // (kappa u_32 >> 1) for GMRES-IR to pay off against an FP64 refactor
+                if (!conv[c] && it == 1 && rn > prev[c]) diverged = true;
                 if (!std::isfinite(rn)) stalled = true;
                 prev[c] = rn;
                 all &= conv[c];
@@ -409,6 +417,9 @@ struct MixedFactor {
             bool all_ok = true;
             for (int c = 0; c < nrhs; c++) all_ok &= conv[c] != 0;
             if (all_ok) return RL_OK;
+            need_fp64 = diverged;
+        }
+        if (!need_fp64) {
             // GMRES-IR on each remaining column
             out.path = RL_PATH_GMRES;
             DevBuf<double> xb, bb;
@@ -456,6 +467,131 @@ inline rl_status solve_mixed(const double *A, long long lda, int n, int kind, co
     MixedFactor mf;
     RL_TRY(mf.factor(A, lda, n, kind, false, s));
     return mf.solve(B, ldb, X, ldx, nrhs, out, s);
+}
+
+// ----------------------------------------------------------------- least squares --
+// min ||A x - b||_2 (m >= n, one right-hand side, device pointers) in FP64: Householder
+// QR of [A | b], then R x = (Q^T b)[0:n] (HouseholderQr composition, qr.rs:250-275).
+inline rl_status lstsq_fp64(const double *A, long long lda, int m, int n, const double *b, double *x, cudaStream_t s) {
+    if (m < n) return RL_ERR_SHAPE;
+    const long long ld = n + 1;
+    DevBuf<double> Ab, tau;
+    DevBuf<int> st;
+    RL_TRY(Ab.alloc((size_t)m * ld, s));
+    RL_TRY(tau.alloc(std::max(1, n), s));
+    RL_TRY(st.alloc(1, s));
+    RL_TRY_CUDA(cudaMemsetAsync(st.p, 0, sizeof(int), s));
+    RL_TRY_CUDA(cudaMemcpy2DAsync(Ab.p, ld * sizeof(double), A, lda * sizeof(double), n * sizeof(double), m,
+                                  cudaMemcpyDeviceToDevice, s));
+    RL_TRY_CUDA(cudaMemcpy2DAsync(Ab.p + n, ld * sizeof(double), b, sizeof(double), sizeof(double), m,
+                                  cudaMemcpyDeviceToDevice, s));
+    RL_TRY(qr_factor_dev<double>(Ab.p, ld, m, (int)ld, n, tau.p, s));
+    RL_TRY(tri_solve_dev<double>(Ab.p, ld, n, Ab.p + n, ld, 1, 2, st.p, s));
+    RL_TRY(read_status<double>(st.p, s));
+    RL_TRY_CUDA(cudaMemcpy2DAsync(x, sizeof(double), Ab.p + n, ld * sizeof(double), sizeof(double), n,
+                                  cudaMemcpyDeviceToDevice, s));
+    return RL_OK;
+}
+
+// g = A^T r for an m x n FP64 matrix (deterministic: fixed chunks, summed in order).
+struct GemvT {
+    double *partial;
+    int chunks, rows_per;
+    rl_status run(const double *A, long long lda, int m, int n, const double *r, double *g, cudaStream_t s) const {
+        RL_LAUNCH(gemv_t_partial_kernel, dim3(ceil_div(n, 256), chunks), 256, 0, s, A, lda, m, n, r, rows_per, partial);
+        RL_LAUNCH(reduce_chunks_kernel, std::min(4 * num_sms(), ceil_div(n, 256)), 256, 0, s, partial, chunks, n, g);
+        return RL_OK;
+    }
+};
+
+// Least squares in mixed precision: Householder QR of the FP32 copy of A gives R with
+// R^T R ~ A^T A; the corrected semi-normal equations refine in FP64,
+//   r = b - A x,  g = A^T r,  x += (R^T R)^-1 g   (R solves in FP32, g scaled),
+// until the correction is below 4u ||x|| (converged to working precision). A correction
+// that does not halve, a pivot of R below FLT_MIN, or ten steps without convergence send
+// the problem to FP64 QR instead. berr reports ||A^T r|| / (||A|| (||A|| ||x|| + ||b||)),
+// inf-norms, for the returned x.
+inline rl_status lstsq_mixed(const double *A, long long lda, int m, int n, const double *b, double *x, SolveOut &out,
+                             cudaStream_t s) {
+    out = SolveOut();
+    if (m < n) return RL_ERR_SHAPE;
+    if (n == 0) return RL_OK;
+    DevBuf<float> Q32, L, tau32, w32;
+    DevBuf<double> r, g, dx, partial;
+    DevBuf<unsigned long long> bits;  // 0 anorm, 1 bnorm, 2 scale, 3 xn, 4 dxn, 5 gn
+    DevBuf<int> dstatus, one;
+    const int rows_per = 256, chunks = ceil_div(m, rows_per);
+    RL_TRY(Q32.alloc((size_t)m * n, s));
+    RL_TRY(L.alloc((size_t)n * n, s));
+    RL_TRY(tau32.alloc(n, s));
+    RL_TRY(w32.alloc(n, s));
+    RL_TRY(r.alloc(m, s));
+    RL_TRY(g.alloc(n, s));
+    RL_TRY(dx.alloc(n, s));
+    RL_TRY(partial.alloc((size_t)chunks * n, s));
+    RL_TRY(bits.alloc(6, s));
+    RL_TRY(dstatus.alloc(1, s));
+    RL_TRY(one.alloc(1, s));
+    RL_TRY_CUDA(cudaMemsetAsync(bits.p, 0, 6 * sizeof(unsigned long long), s));
+    RL_TRY_CUDA(cudaMemsetAsync(dstatus.p, 0, sizeof(int), s));
+    const int h_one = 1;
+    RL_TRY_CUDA(cudaMemcpyAsync(one.p, &h_one, sizeof(int), cudaMemcpyHostToDevice, s));
+    RL_LAUNCH(to_f32_rect_kernel, grid_rows(m, 8), 256, 0, s, A, lda, m, n, Q32.p, (long long)n, bits.p);
+    RL_TRY(colnorm_dev(b, 1, m, 1, bits.p + 1, s));
+    RL_TRY(qr_factor_dev<float>(Q32.p, n, m, n, n, tau32.p, s));
+    RL_LAUNCH(upper_to_lower_t_kernel, (int)std::min<long long>(8 * num_sms(), ((long long)n * n + 255) / 256), 256, 0, s,
+              Q32.p, (long long)n, n, L.p);
+    Minv M{L.p, n, RL_KIND_CHOLESKY, nullptr, w32.p, bits.p + 2, one.p, dstatus.p};
+    GemvT At{partial.p, chunks, rows_per};
+    const int gv = std::min(4 * num_sms(), ceil_div(n, 256));
+    // x0 = (R^T R)^-1 A^T b
+    RL_TRY(At.run(A, lda, m, n, b, g.p, s));
+    RL_TRY(M.apply(g.p, x, s));
+    bool ok = false;
+    double prev = INFINITY, anorm = 0.0, bnorm = 0.0, xn = 0.0;
+    for (int it = 0; it < 10; it++) {
+        RL_LAUNCH(resid_rect_kernel, grid_rows(m, 8), 256, 0, s, A, lda, m, n, x, b, r.p);
+        RL_TRY(At.run(A, lda, m, n, r.p, g.p, s));
+        RL_TRY(M.apply(g.p, dx.p, s));
+        RL_LAUNCH(add_kernel, gv, 256, 0, s, x, dx.p, n);
+        RL_TRY(colnorm_dev(x, 1, n, 1, bits.p + 3, s));
+        RL_TRY(colnorm_dev(dx.p, 1, n, 1, bits.p + 4, s));
+        unsigned long long hb[5];
+        int dst = 0;
+        RL_TRY_CUDA(cudaMemcpyAsync(hb, bits.p, sizeof hb, cudaMemcpyDeviceToHost, s));
+        RL_TRY_CUDA(cudaMemcpyAsync(&dst, dstatus.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+        RL_TRY_CUDA(cudaStreamSynchronize(s));
+        anorm = bits_to_double(hb[0]);
+        bnorm = bits_to_double(hb[1]);
+        xn = bits_to_double(hb[3]);
+        const double dn = bits_to_double(hb[4]);
+        out.iters = it + 1;
+        if (dst != 0 || !std::isfinite(dn)) break;
+        if (dn <= 4.0 * kU * xn) {
+            ok = true;
+            break;
+        }
+        if (it >= 1 && dn > 0.5 * prev) break;
+        prev = dn;
+    }
+    if (!ok) {
+        out.path = RL_PATH_FP64;
+        RL_TRY(lstsq_fp64(A, lda, m, n, b, x, s));
+        RL_TRY(colnorm_dev(x, 1, n, 1, bits.p + 3, s));
+    }
+    // reported quality: the normal-equations residual of the returned x
+    RL_LAUNCH(resid_rect_kernel, grid_rows(m, 8), 256, 0, s, A, lda, m, n, x, b, r.p);
+    RL_TRY(At.run(A, lda, m, n, r.p, g.p, s));
+    RL_TRY(colnorm_dev(g.p, 1, n, 1, bits.p + 5, s));
+    unsigned long long hb[6];
+    RL_TRY_CUDA(cudaMemcpyAsync(hb, bits.p, sizeof hb, cudaMemcpyDeviceToHost, s));
+    RL_TRY_CUDA(cudaStreamSynchronize(s));
+    anorm = bits_to_double(hb[0]);
+    bnorm = bits_to_double(hb[1]);
+    xn = bits_to_double(hb[3]);
+    const double den = anorm * (anorm * xn + bnorm);
+    out.berr = den > 0 ? bits_to_double(hb[5]) / den : 0.0;
+    return RL_OK;
 }
 
 }  // namespace rl

@@ -79,7 +79,8 @@ size_t footprint(const rl_request &r) {
     const size_t n = r.n, m = r.m ? r.m : r.n;
     switch (r.kind) {
         case RL_REQ_RESOLVE: return 32 * n + 4096;
-        case RL_REQ_LSTSQ: return 8 * m * (n + 1) + 8 * m * 64 + 64 * n * 16 + 4096;
+        // A (f64), its FP32 QR, R^T, panel buffers, vectors, and the FP64 [A | b] of the fallback
+        case RL_REQ_LSTSQ: return 8 * m * n + 4 * m * n + 4 * n * n + 8 * m * 64 + 64 * n * 16 + 8 * m * (n + 2) + 4096;
         default: return 8 * n * n + 4 * n * n + 48 * n + 4096;  // A (f64), FP32 factor, vectors
     }
 }
@@ -303,31 +304,26 @@ struct Worker {
         return solve_with(*res->f, q);
     }
 
-    // min ||A x - b|| (m >= n) through Householder QR of [A | b] in FP64.
+    // min ||A x - b|| (m >= n) through the mixed-precision least-squares solver (FP32
+    // QR, FP64 semi-normal-equation refinement, FP64 QR fallback).
     rl_status run_lstsq(Req *q) {
         cudaStream_t st = stream;
         const rl_request &r = q->r;
         const int m = (int)r.m, n = (int)r.n;
         if (m < n) return RL_ERR_SHAPE;
-        const long long ld = n + 1;
-        DevBuf<double> dA, tau;
-        DevBuf<int> stt;
-        RL_TRY(dA.alloc((size_t)m * ld, st));
-        RL_TRY(tau.alloc(std::max(1, n), st));
-        RL_TRY(stt.alloc(1, st));
-        RL_TRY_CUDA(cudaMemsetAsync(stt.p, 0, sizeof(int), st));
-        RL_TRY_CUDA(cudaMemcpy2DAsync(dA.p, ld * sizeof(double), r.a, n * sizeof(double), n * sizeof(double), m,
-                                      cudaMemcpyHostToDevice, st));
-        RL_TRY_CUDA(cudaMemcpy2DAsync(dA.p + n, ld * sizeof(double), r.b, sizeof(double), sizeof(double), m,
-                                      cudaMemcpyHostToDevice, st));
-        RL_TRY(qr_factor_dev<double>(dA.p, ld, m, (int)ld, n, tau.p, st));
-        RL_TRY(tri_solve_dev<double>(dA.p, ld, n, dA.p + n, ld, 1, 2, stt.p, st));
-        RL_TRY(read_status<double>(stt.p, st));
-        RL_TRY_CUDA(cudaMemcpy2DAsync(r.x, sizeof(double), dA.p + n, ld * sizeof(double), sizeof(double), n,
-                                      cudaMemcpyDeviceToHost, st));
+        DevBuf<double> dA, db, dx;
+        RL_TRY(dA.alloc((size_t)m * n, st));
+        RL_TRY(db.alloc(m, st));
+        RL_TRY(dx.alloc(n, st));
+        RL_TRY_CUDA(cudaMemcpyAsync(dA.p, r.a, (size_t)m * n * sizeof(double), cudaMemcpyHostToDevice, st));
+        RL_TRY_CUDA(cudaMemcpyAsync(db.p, r.b, (size_t)m * sizeof(double), cudaMemcpyHostToDevice, st));
+        SolveOut o;
+        RL_TRY(lstsq_mixed(dA.p, n, m, n, db.p, dx.p, o, st));
+        RL_TRY_CUDA(cudaMemcpyAsync(r.x, dx.p, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, st));
         RL_TRY_CUDA(cudaStreamSynchronize(st));
-        q->res.path = RL_PATH_FP64;
-        q->res.berr = 0.0;
+        q->res.iters = o.iters;
+        q->res.path = o.path;
+        q->res.berr = o.berr;
         return RL_OK;
     }
 
