@@ -373,7 +373,14 @@ def serve_workload(args, rank, world, dev):
             st = srv.stats()
             ok = sum(1 for r in res if r["status"] == 0)
             berrs = [r["berr"] for r, q in zip(res, reqs) if q[0] != rl.REQ_LSTSQ]
-            runs.append({"lambda": lam, "requests": count, "ok": ok, "p50_ms": st["p50_us"] / 1e3,
+            by_kind = {}
+            names = {rl.REQ_LU: "lu", rl.REQ_CHOLESKY: "cholesky", rl.REQ_LSTSQ: "lstsq", rl.REQ_RESOLVE: "resolve"}
+            for k, nm in names.items():
+                lat = sorted(r["latency_us"] / 1e3 for r, q in zip(res, reqs) if q[0] == k)
+                if lat:
+                    by_kind[nm] = {"count": len(lat), "p50_ms": lat[len(lat) // 2],
+                                   "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))]}
+            runs.append({"lambda": lam, "requests": count, "ok": ok, "by_kind": by_kind, "p50_ms": st["p50_us"] / 1e3,
                          "p99_ms": st["p99_us"] / 1e3, "mean_ms": st["mean_us"] / 1e3,
                          "solves_per_s": st["solves_per_s"], "wall_s": wall, "batches": st["batches"],
                          "batched_requests": st["batched_requests"], "bytes_peak": st["bytes_peak"],

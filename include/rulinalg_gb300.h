@@ -246,7 +246,7 @@ RL_API rl_status rl_dlstsq_mixed(size_t m, size_t n, const double *a, size_t lda
 typedef struct rl_server rl_server;
 typedef struct rl_server_config {
     size_t hbm_budget_bytes; /* 0: 80% of the free device memory after start-up */
-    int workers;             /* worker threads / CUDA streams (0: 4) */
+    int workers;             /* worker threads / CUDA streams (0: 8); worker 0 serves only batchable requests */
     int max_batch;           /* systems per batched launch (0: 4096) */
     int small_n;             /* largest n sent to the batched kernel (0: 512) */
 } rl_server_config;

@@ -6,6 +6,8 @@
 
 #include <climits>
 
+#include <cooperative_groups.h>
+
 #include "factor_cta.cuh"
 
 namespace rl {
@@ -197,6 +199,132 @@ static __global__ void __launch_bounds__(256) lu_panel_kernel(T *P, long long ld
     }
 }
 
+// LU panel on one thread-block cluster (up to 16 CTAs): the same algorithm as
+// lu_panel_kernel with the cross-CTA exchange moved on chip. CTA q owns rows
+// [q * rows_per, ...) in shared memory; per column every CTA publishes its candidate
+// (|v|, row, the row's values) and, if it holds it, row j in its own shared memory, one
+// cluster barrier makes them visible, and every CTA reads the candidates of all CTAs
+// through distributed shared memory and picks the same winner. Candidate slots are
+// double-buffered by column parity, so one barrier per column suffices. Every CTA runs
+// the same number of barriers (a failing pivot is seen by all at the same column) and
+// a last barrier keeps each CTA's shared memory alive until no other CTA reads it.
+template <class T>
+static __global__ void __launch_bounds__(256) lu_panel_cluster_kernel(T *P, long long lda, int mrows, int kb, int k0,
+                                                              int rows_per, int *ipiv, int *err, T tiny) {
+    namespace cg = cooperative_groups;
+    constexpr int NB = PanelNB<T>::value;
+    constexpr int LDR = NB + 1;
+    constexpr int CS = 2 + NB;  // candidate record: |v|, row, then the row's values
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *R = reinterpret_cast<T *>(smem_raw);    // rows_per x LDR
+    T *cand = R + (size_t)rows_per * LDR;      // 2 x CS, this CTA's candidate per parity
+    T *rowj = cand + 2 * CS;                   // 2 x NB, row j when this CTA holds it
+    T *prow = rowj + 2 * NB;                   // NB, the pivot row
+    __shared__ T s_v[8];
+    __shared__ int s_i[8], s_q[8];
+    cg::cluster_group cluster = cg::this_cluster();
+    const int C = (int)cluster.num_blocks(), g = (int)cluster.block_rank();
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int r0 = g * rows_per, r1 = min(mrows, r0 + rows_per), nr = max(0, r1 - r0);
+    if (g == 0)
+        for (int j = tid; j < kb; j += blockDim.x) ipiv[j] = k0 + j;
+    for (int idx = tid; idx < nr * kb; idx += blockDim.x) {
+        const int r = idx / kb, c = idx - r * kb;
+        R[r * LDR + c] = P[(long long)(r0 + r) * lda + c];
+    }
+    __syncthreads();
+    for (int j = 0; j < kb; j++) {
+        const int slot = j & 1;
+        // local candidate
+        T bv = T(-1);
+        int bi = INT_MAX;
+        for (int r = max(j - r0, 0) + tid; r < nr; r += blockDim.x) {
+            const T v = absT(R[r * LDR + j]);
+            if (v > bv) {
+                bv = v;
+                bi = r0 + r;
+            }
+        }
+        warp_amax(bv, bi);
+        if (lane == 0) {
+            s_v[warp] = bv;
+            s_i[warp] = bi;
+        }
+        __syncthreads();
+        bv = s_v[0];
+        bi = s_i[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) amax_combine(bv, bi, s_v[w], s_i[w]);
+        T *mine = cand + slot * CS;
+        if (tid == 0) {
+            mine[0] = bv;
+            mine[1] = (T)(bi == INT_MAX ? -1 : bi);
+        }
+        if (bi != INT_MAX && tid < kb) mine[2 + tid] = R[(bi - r0) * LDR + tid];
+        if (j >= r0 && j < r1 && tid < kb) rowj[slot * NB + tid] = R[(j - r0) * LDR + tid];
+        cluster.sync();
+        // the winner over the cluster, identical in every CTA (warp 0: lane q reads CTA q)
+        if (warp == 0) {
+            T wv = T(-1);
+            int wi = INT_MAX, wg = -1;
+            if (lane < C) {
+                const T *c = cluster.map_shared_rank(cand + slot * CS, lane);
+                const T v = c[0];
+                const int i = (int)c[1];
+                if (i >= 0) {
+                    wv = v;
+                    wi = i;
+                    wg = lane;
+                }
+            }
+            warp_amax3(wv, wi, wg);
+            if (lane == 0) {
+                s_v[0] = wv;
+                s_i[0] = wi;
+                s_q[0] = wg;
+            }
+        }
+        __syncthreads();
+        const T wv = s_v[0];
+        int wi = s_i[0], wg = s_q[0];
+        if (wi == INT_MAX) {  // no finite candidate (NaN column): keep the diagonal
+            wi = j;
+            wg = -1;
+        }
+        const bool stop = wg >= 0 && wv < tiny;  // the same decision in every CTA
+        const int owner_j = j / rows_per;        // the CTA holding row j
+        if (!stop && tid < kb) {
+            const T *src = wg >= 0 ? cluster.map_shared_rank(cand + slot * CS, wg) + 2
+                                   : cluster.map_shared_rank(rowj + slot * NB, owner_j);
+            prow[tid] = src[tid];
+        }
+        if (stop) {
+            if (g == 0 && tid == 0) atomicCAS(err, 0, RL_ERR_DIV_BY_ZERO);
+            break;
+        }
+        __syncthreads();
+        if (wi != j) {
+            if (j >= r0 && j < r1 && tid < kb) R[(j - r0) * LDR + tid] = prow[tid];
+            if (wi >= r0 && wi < r1 && tid < kb)
+                R[(wi - r0) * LDR + tid] = cluster.map_shared_rank(rowj + slot * NB, owner_j)[tid];
+        }
+        if (g == 0 && tid == 0) ipiv[j] = k0 + wi;
+        __syncthreads();
+        const T p = prow[j];
+        for (int r = max(j + 1 - r0, 0) + tid; r < nr; r += blockDim.x) {
+            T *row = R + r * LDR;
+            const T l = row[j] / p;
+            row[j] = l;
+            for (int c = j + 1; c < kb; c++) row[c] = fma(-l, prow[c], row[c]);
+        }
+        __syncthreads();
+    }
+    for (int idx = tid; idx < nr * kb; idx += blockDim.x) {
+        const int r = idx / kb, c = idx - r * kb;
+        P[(long long)(r0 + r) * lda + c] = R[r * LDR + c];
+    }
+    cluster.sync();  // no CTA leaves while another may still read its shared memory
+}
+
 // ------------------------------------------------------------ Householder panel --
 // Unblocked Householder QR of the panel rows [0, mrows) x cols [0, kb) (P points at
 // A[k0][k0]), reflector by reflector exactly as HouseholderReflection::compute and
@@ -297,6 +425,108 @@ static __global__ void __launch_bounds__(256) qr_panel_kernel(T *P, long long ld
         const int r = idx / kb, c = idx - r * kb;
         P[(long long)(r0 + r) * lda + c] = R[r * LDR + c];
     }
+}
+
+// Householder panel on one thread-block cluster (up to 16 CTAs): qr_panel_kernel's
+// algorithm with the two cross-CTA sums per column (sigma, then u = A^T v) read from
+// the other CTAs' shared memory after a cluster barrier. The sums run over the CTAs in
+// rank order in every CTA, so every CTA computes the same tau and u. A column with
+// sigma = 0 still passes a second barrier, so every CTA runs the same barrier sequence,
+// and a last barrier keeps shared memory alive until no other CTA reads it.
+template <class T>
+static __global__ void __launch_bounds__(256) qr_panel_cluster_kernel(T *P, long long lda, int mrows, int kb,
+                                                              int rows_per, T *tau) {
+    namespace cg = cooperative_groups;
+    constexpr int NB = PanelNB<T>::value;
+    constexpr int LDR = NB + 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *R = reinterpret_cast<T *>(smem_raw);  // rows_per x LDR
+    T *u = R + (size_t)rows_per * LDR;       // NB: this column's u (all CTAs)
+    T *upart = u + NB;                       // NB: this CTA's partial of u
+    T *misc = upart + NB;                    // [0] this CTA's sigma partial, [1] x0 (owner of row j)
+    __shared__ T s_red[8];
+    cg::cluster_group cluster = cg::this_cluster();
+    const int C = (int)cluster.num_blocks(), g = (int)cluster.block_rank();
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nw = blockDim.x >> 5;
+    const int r0 = g * rows_per, r1 = min(mrows, r0 + rows_per), nr = max(0, r1 - r0);
+    for (int idx = tid; idx < nr * kb; idx += blockDim.x) {
+        const int r = idx / kb, c = idx - r * kb;
+        R[r * LDR + c] = P[(long long)(r0 + r) * lda + c];
+    }
+    __syncthreads();
+    for (int j = 0; j < kb; j++) {
+        const int owner_j = j / rows_per;
+        // (1) sigma partial over rows > j
+        T sp = T(0);
+        for (int r = max(j + 1 - r0, 0) + tid; r < nr; r += blockDim.x) {
+            const T v = R[r * LDR + j];
+            sp = fma(v, v, sp);
+        }
+        sp = warp_sum(sp);
+        if (lane == 0) s_red[warp] = sp;
+        __syncthreads();
+        if (tid == 0) {
+            T t = T(0);
+            for (int w = 0; w < nw; w++) t += s_red[w];
+            misc[0] = t;
+            if (j >= r0 && j < r1) misc[1] = R[(j - r0) * LDR + j];
+        }
+        cluster.sync();
+        // sigma over the CTAs in rank order (lane q reads CTA q), x0 from row j's owner
+        T sigma = T(0);
+        if (warp == 0) {
+            sigma = lane < C ? cluster.map_shared_rank(misc, lane)[0] : T(0);
+            sigma = warp_sum(sigma);
+            if (lane == 0) s_red[0] = sigma;
+        }
+        __syncthreads();
+        sigma = s_red[0];
+        const T x0 = cluster.map_shared_rank(misc, owner_j)[1];
+        if (sigma == T(0)) {  // already a multiple of e1: tau = 0, nothing changes
+            if (g == 0 && tid == 0) tau[j] = T(0);
+            cluster.sync();
+            continue;
+        }
+        const T x_norm = sqrt(x0 * x0 + sigma);
+        const T v0 = x0 > T(0) ? x0 + x_norm : x0 - x_norm;
+        const T two = T(2);
+        const T t = two * v0 * v0 / (v0 * v0 + sigma);
+        if (g == 0 && tid == 0) tau[j] = t;
+        // (2) u_c partial = sum_r v_r a[r][c] for c >= j over owned rows r >= j
+        for (int c = j + warp; c < kb; c += nw) {
+            T acc = T(0);
+            for (int r = max(j - r0, 0) + lane; r < nr; r += 32) {
+                const T vr = (r0 + r == j) ? T(1) : R[r * LDR + j] / v0;
+                acc = fma(vr, R[r * LDR + c], acc);
+            }
+            acc = warp_sum(acc);
+            if (lane == 0) upart[c] = acc;
+        }
+        cluster.sync();
+        if (tid >= j && tid < kb) {
+            T a = T(0);
+            for (int q = 0; q < C; q++) a += cluster.map_shared_rank(upart, q)[tid];
+            u[tid] = a;
+        }
+        __syncthreads();
+        // (3) a[r][c] += (-tau v_r) u_c for c > j; the diagonal becomes x0 - tau u_j and
+        // v[1..] is stored below it
+        for (int r = max(j - r0, 0) + tid; r < nr; r += blockDim.x) {
+            T *row = R + r * LDR;
+            const bool diag = (r0 + r == j);
+            const T vr = diag ? T(1) : row[j] / v0;
+            const T sc = -t * vr;
+            for (int c = j + 1; c < kb; c++) row[c] = fma(sc, u[c], row[c]);
+            row[j] = diag ? x0 - t * u[j] : vr;
+        }
+        __syncthreads();
+    }
+    for (int idx = tid; idx < nr * kb; idx += blockDim.x) {
+        const int r = idx / kb, c = idx - r * kb;
+        P[(long long)(r0 + r) * lda + c] = R[r * LDR + c];
+    }
+    cluster.sync();  // no CTA leaves while another may still read its shared memory
 }
 
 // ------------------------------------------------------------------- row swaps --

@@ -59,7 +59,104 @@ rl_status launch_coop(void *kern, int G, size_t smem, void **args, cudaStream_t 
     return RL_OK;
 }
 
-// Blocked right-looking LU for any n: cooperative panel, row swaps, U12 solve, GEMM.
+// Largest thread-block cluster (16 or 8 CTAs, 0: none) on which `kern` can run with
+// `smem` bytes of dynamic shared memory per CTA; sets the kernel's attributes.
+template <class K>
+int probe_cluster(K kern, size_t smem) {
+    int found = 0;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess) {
+        for (int c : {16, 8}) {
+            cudaLaunchConfig_t cfg = {};
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = c;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.gridDim = dim3(c);
+            cfg.blockDim = dim3(256);
+            cfg.dynamicSmemBytes = smem;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            int nclusters = 0;
+            if (cudaOccupancyMaxActiveClusters(&nclusters, kern, &cfg) == cudaSuccess && nclusters >= 1) {
+                found = c;
+                break;
+            }
+        }
+    }
+    cudaGetLastError();  // a refused query is not an error of the factorisation
+    return found;
+}
+
+// Cluster size and rows per CTA for a panel of mrows rows of row_bytes each plus `extra`
+// bytes per CTA: the fewest CTAs with at most kClusterSmem bytes each (and at least
+// ceil(mrows / 256) CTAs), or 0 when that exceeds cmax.
+constexpr size_t kClusterSmem = 200 * 1024;
+inline int cluster_shape(int mrows, size_t row_bytes, size_t extra, int cmax, int &rows_per) {
+    const int cmin = (int)(((size_t)mrows * row_bytes + (kClusterSmem - extra) - 1) / (kClusterSmem - extra));
+    int C = std::max(cmin, ceil_div(mrows, 256));
+    if (C > cmax) return 0;
+    C = std::max(C, 2);
+    rows_per = ceil_div(mrows, C);
+    return C;
+}
+
+template <class K, class... Args>
+rl_status launch_cluster(K kern, int C, size_t smem, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(C);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    RL_TRY_CUDA(cudaLaunchKernelEx(&cfg, kern, args...));
+    count_launch();
+    return RL_OK;
+}
+
+// The LU panel on one cluster when it fits (launched = true), else nothing.
+template <class T>
+rl_status lu_panel_cluster(T *P, long long lda, int mrows, int kb, int k0, int *ipiv, int *err, T tiny, cudaStream_t s,
+                           bool &launched) {
+    constexpr int NB = PanelNB<T>::value;
+    launched = false;
+    auto kern = lu_panel_cluster_kernel<T>;
+    static const int cmax = probe_cluster(kern, kClusterSmem);
+    const size_t row_bytes = (NB + 1) * sizeof(T), extra = (2 * (2 + NB) + 3 * NB) * sizeof(T);
+    int rows_per = 0;
+    const int C = cluster_shape(mrows, row_bytes, extra, cmax, rows_per);
+    if (C == 0) return RL_OK;
+    RL_TRY(launch_cluster(kern, C, (size_t)rows_per * row_bytes + extra, s, P, lda, mrows, kb, k0, rows_per, ipiv, err,
+                          tiny));
+    launched = true;
+    return RL_OK;
+}
+
+// The Householder panel on one cluster when it fits (launched = true), else nothing.
+template <class T>
+rl_status qr_panel_cluster(T *P, long long lda, int mrows, int kb, T *tau, cudaStream_t s, bool &launched) {
+    constexpr int NB = PanelNB<T>::value;
+    launched = false;
+    auto kern = qr_panel_cluster_kernel<T>;
+    static const int cmax = probe_cluster(kern, kClusterSmem);
+    const size_t row_bytes = (NB + 1) * sizeof(T), extra = (2 * NB + 2) * sizeof(T);
+    int rows_per = 0;
+    const int C = cluster_shape(mrows, row_bytes, extra, cmax, rows_per);
+    if (C == 0) return RL_OK;
+    RL_TRY(launch_cluster(kern, C, (size_t)rows_per * row_bytes + extra, s, P, lda, mrows, kb, rows_per, tau));
+    launched = true;
+    return RL_OK;
+}
+
+// Blocked right-looking LU for any n: panel (one cluster, or a cooperative grid for
+// panels too tall for a cluster), row swaps, U12 solve, GEMM.
 template <class T>
 rl_status lu_factor_dev(T *A, long long lda, int n, int *ipiv, cudaStream_t s, T tiny = Eps<T>::value) {
     if (n <= 0) return RL_OK;
@@ -86,11 +183,15 @@ rl_status lu_factor_dev(T *A, long long lda, int n, int *ipiv, cudaStream_t s, T
         int G, rows_per;
         panel_geometry<T>(mrows, G, rows_per);
         const size_t smem = ((size_t)rows_per * (NB + 1) + NB) * sizeof(T);
-        if (k0 > 0) RL_TRY_CUDA(cudaMemsetAsync(&sync.p->ctr, 0, sizeof(unsigned), s));
         T *P = A + (long long)k0 * lda + k0;
         int *ip = ipiv + k0;
-        void *args[] = {&P, &lda, (void *)&mrows, (void *)&kb, &k0, &rows_per, &ip, &cand.p, &rowj.p, &sync.p, &tiny};
-        RL_TRY(launch_coop<T>((void *)pk, G, smem, args, s));
+        bool clustered = false;
+        RL_TRY(lu_panel_cluster<T>(P, lda, mrows, kb, k0, ip, &sync.p->err, tiny, s, clustered));
+        if (!clustered) {
+            if (k0 > 0) RL_TRY_CUDA(cudaMemsetAsync(&sync.p->ctr, 0, sizeof(unsigned), s));
+            void *args[] = {&P, &lda, (void *)&mrows, (void *)&kb, &k0, &rows_per, &ip, &cand.p, &rowj.p, &sync.p, &tiny};
+            RL_TRY(launch_coop<T>((void *)pk, G, smem, args, s));
+        }
         const int nother = n - kb;
         if (nother > 0)
             RL_LAUNCH(laswp_kernel<T>, ceil_div(nother, 256), 256, 0, s, A, lda, n, k0, k0 + kb, ipiv, k0, k0 + kb);
@@ -159,11 +260,15 @@ rl_status qr_factor_dev(T *A, long long lda, int m, int n, int nrefl, T *tau, cu
         int G, rows_per;
         panel_geometry<T>(mrows, G, rows_per);
         const size_t smem = ((size_t)rows_per * (NB + 1) + NB) * sizeof(T);
-        if (k0 > 0) RL_TRY_CUDA(cudaMemsetAsync(&sync.p->ctr, 0, sizeof(unsigned), s));
         T *P = A + (long long)k0 * lda + k0;
         T *tk = tau + k0;
-        void *args[] = {&P, &lda, (void *)&mrows, (void *)&kb, &rows_per, &tk, &part.p, &x0buf.p, &sync.p};
-        RL_TRY(launch_coop<T>((void *)pk, G, smem, args, s));
+        bool clustered = false;
+        RL_TRY(qr_panel_cluster<T>(P, lda, mrows, kb, tk, s, clustered));
+        if (!clustered) {
+            if (k0 > 0) RL_TRY_CUDA(cudaMemsetAsync(&sync.p->ctr, 0, sizeof(unsigned), s));
+            void *args[] = {&P, &lda, (void *)&mrows, (void *)&kb, &rows_per, &tk, &part.p, &x0buf.p, &sync.p};
+            RL_TRY(launch_coop<T>((void *)pk, G, smem, args, s));
+        }
         const int n2 = n - k0 - kb;
         if (n2 <= 0) continue;
         const long long mk = (long long)mrows * kb;

@@ -1,18 +1,22 @@
 // One-CTA dense factorisations and solves for systems with n <= CTA_NMAX (512).
 //
-// A CTA of CTA_THREADS threads owns one matrix that lives in global memory (L2-resident
-// at these sizes) and runs a right-looking blocked algorithm over it:
-//   * the current column panel (rows k0..n, NB columns) is staged in shared memory
-//     column-major, factored there column by column (block-wide warp-shuffle argmax for
-//     the LU pivot, first maximum on ties as in PartialPivLu::decompose,
-//     src/matrix/decomposition/lu.rs:169-178), and written back;
-//   * the panel's row swaps are applied to the other columns with each thread owning
-//     whole columns, so rows move as contiguous (coalesced) runs;
-//   * L11^-1 is formed once per panel (warp-shuffle forward substitution); per 64-column
-//     slice, U12 = L11^-1 A12 is a small shared-memory GEMM, followed by the trailing
-//     update A22 -= L21 U12 as 64x64 register-tiled blocks with L21 read from the
-//     shared-memory panel.
-// Cholesky uses the same panel machinery (the panel is the whole column block, so the
+// A CTA of CTA_THREADS threads owns one matrix that lives in global memory (its slot of
+// the batch workspace, or the caller's buffer) and runs a right-looking blocked
+// algorithm over it:
+//   * the current column panel (rows k0..n, NB columns) is held in registers, two rows
+//     per thread, and factored column by column in a rolled loop over a rotated panel
+//     (row[k][0] is always the current column), with one barrier per column: warp
+//     argmax on the hardware redux instructions for the LU pivot, first maximum on
+//     ties as in PartialPivLu::decompose (src/matrix/decomposition/lu.rs:169-178);
+//     rows keep their registers and only their positions move, so each row is written
+//     once, at its final position (shared-memory panel for the update, global memory);
+//   * the rows whose position changed are moved in the other columns through a
+//     shared-memory stage, all loads in flight;
+//   * L11^-1 is formed once per panel (warp-shuffle forward substitution); per
+//     128-column slice, U12 = L11^-1 A12 is a small shared-memory GEMM, followed by the
+//     trailing update A22 -= L21 U12 as 64x64 register-tiled blocks with L21 read from
+//     the shared-memory panel.
+// Cholesky uses the same register panel (the panel is the whole column block, so the
 // diagonal block and L21 are factored together) followed by a lower-triangle SYRK.
 // The factor type T is float (mixed precision) or double (plain FP64).
 #pragma once
@@ -55,24 +59,12 @@ struct CtaOcc<double> {
     static constexpr int value = 2;
 };
 
-// Elements of the staged trailing-update C tile (64 x 64, FP32 only: the FP64 workspace
-// has no room for it at two CTAs per SM).
-template <class T>
-struct CtaStage {
-    static constexpr int value = 1;
-};
-template <>
-struct CtaStage<float> {
-    static constexpr int value = 64 * 64;
-};
-
 // Shared-memory workspace of one CTA (dynamic shared memory).
 template <class T>
 struct CtaSmem {
     // Every array starts on a 16-byte boundary (128-bit shared-memory accesses).
     static constexpr int NB = CtaNB<T>::value;
     alignas(16) T P[NB * CTA_LDP];     // panel, column-major: P[c * CTA_LDP + r]
-    alignas(16) T Cst[CtaStage<T>::value];  // the next trailing-update C tile, copied in asynchronously
     union alignas(16) {
         T Bt[NB * 128];            // factorisation: one 128-column slice of U12, row-swap staging
         double xr[2 * CTA_NMAX];   // refinement (after the factorisation): FP64 x, then FP64 r
@@ -389,81 +381,6 @@ __device__ __forceinline__ void update_tile(T *__restrict__ A, int lda, int k0, 
     }
 }
 
-// cp.async (16 bytes, L2 only) with zero fill past src_bytes.
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, int src_bytes) {
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "r"(src_bytes) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
-
-// Starts the copy of this thread's 4 x 4 fragment of the C tile at (row0, col0) into its
-// own slots of Cst (rows past mrows and columns past lim(row, col) read as zero).
-template <class Lim>
-__device__ __forceinline__ void stage_tile(const float *__restrict__ A, int lda, int k0, int mrows, int row0, int col0,
-                                           Lim lim, float *Cst) {
-    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        const int r = row0 + ty * 4 + i, c = col0 + tx * 4;
-        int nb = 0;
-        const float *src = A;  // any valid address when nothing is read
-        if (r < mrows) {
-            nb = 4 * max(0, min(4, lim(r, c)));
-            if (nb > 0) src = A + (long long)(k0 + r) * lda + k0 + c;
-        }
-        cp_async16(&Cst[(ty * 4 + i) * 64 + tx * 4], src, nb);
-    }
-    cp_async_commit();
-}
-
-// The FP32 trailing update over a list of 64 x 64 tiles (tile(t, row0, col0, bcol0) as
-// in update_tile) with the next tile's C copied in asynchronously while the current one
-// is computed, so the global latency is paid once per list. Every row start must be
-// 16-byte aligned. Each thread reads back only the slots it copied itself, and re-stages
-// them only after the first k-step has consumed them, so no barrier is needed.
-template <int NB, class TileFn, class Lim>
-__device__ void update_tiles_staged(float *__restrict__ A, int lda, int k0, int mrows, int ntiles, TileFn tile,
-                                    const float *__restrict__ P, const float *__restrict__ bs, int ldb, Lim lim,
-                                    float *Cst, bool first_staged) {
-    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    if (ntiles <= 0) return;
-    int row0, col0, bcol0;
-    tile(0, row0, col0, bcol0);
-    if (!first_staged) stage_tile(A, lda, k0, mrows, row0, col0, lim, Cst);
-    for (int t = 0; t < ntiles; t++) {
-        cp_async_wait_all();
-        float cv[4][4];
-#pragma unroll
-        for (int i = 0; i < 4; i++) ld4<float>(&Cst[(ty * 4 + i) * 64 + tx * 4], cv[i]);
-        auto step = [&](int p) {
-            float a[4], b[4];
-            ld4<float>(&P[p * CTA_LDP + row0 + ty * 4], a);
-            ld4<float>(&bs[p * ldb + bcol0 + tx * 4], b);
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-#pragma unroll
-                for (int j = 0; j < 4; j++) cv[i][j] = fma(-a[i], b[j], cv[i][j]);
-        };
-        step(0);
-        int nrow0 = 0, ncol0 = 0, nbcol0 = 0;
-        if (t + 1 < ntiles) {
-            tile(t + 1, nrow0, ncol0, nbcol0);
-            stage_tile(A, lda, k0, mrows, nrow0, ncol0, lim, Cst);
-        }
-#pragma unroll 3
-        for (int p = 1; p < NB; p++) step(p);
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-            const int r = row0 + ty * 4 + i, c = col0 + tx * 4;
-            if (r < mrows) gst4(A + (long long)(k0 + r) * lda + k0 + c, cv[i], lim(r, c), true);
-        }
-        row0 = nrow0;
-        col0 = ncol0;
-        bcol0 = nbcol0;
-    }
-}
-
 // ---------------------------------------------------------------------------- LU --
 // Factors the n x n matrix A (row stride lda) in place; S.piv receives the pivots.
 // A pivot with |p| < tiny returns RL_ERR_DIV_BY_ZERO (tiny = epsilon reproduces the
@@ -669,21 +586,7 @@ __device__ int cta_lu_factor(T *__restrict__ A, int lda, int n, CtaSmem<T> &S, T
         const int m2 = mrows - kb;
         constexpr int RPS = NB / 2;  // U12 rows per thread in the slice solve
         for (int tj = 0; tj < n2; tj += 128) {
-            const int nr = (m2 + 63) / 64, nc = (min(128, n2 - tj) + 63) / 64;
-            auto tile = [&](int t, int &r0, int &c0, int &b0) {
-                const int ti = t / nc, tc = t - ti * nc;
-                r0 = kb + ti * 64;
-                c0 = kb + tj + tc * 64;
-                b0 = tc * 64;
-            };
             auto lim = [&](int, int c) { return kb + n2 - c; };
-            if constexpr (CtaStage<T>::value > 1) {
-                if (vec) {  // the slice's first C tile streams in while U12 is formed
-                    int r0, c0, b0;
-                    tile(0, r0, c0, b0);
-                    stage_tile(A, lda, k0, mrows, r0, c0, lim, S.Cst);
-                }
-            }
             {
                 constexpr int K = NB * 128 / CTA_THREADS;
                 T v[K];
@@ -715,19 +618,10 @@ __device__ int cta_lu_factor(T *__restrict__ A, int lda, int n, CtaSmem<T> &S, T
                 }
             }
             __syncthreads();
-            bool done = false;
-            if constexpr (CtaStage<T>::value > 1) {
-                if (vec) {
-                    update_tiles_staged<NB>(A, lda, k0, mrows, nr * nc, tile, S.P, S.u.Bt, 128, lim, S.Cst, true);
-                    done = true;
-                }
-            }
-            if (!done) {
-                constexpr int TS = TileCfg<T>::TS;
-                for (int ti = 0; ti < m2; ti += TS)
-                    for (int tc = 0; tc < 128 && tj + tc < n2; tc += TS)
-                        update_tile<T, NB>(A, lda, k0, mrows, kb + ti, kb + tj + tc, S.P, S.u.Bt, 128, tc, vec, lim);
-            }
+            constexpr int TS = TileCfg<T>::TS;
+            for (int ti = 0; ti < m2; ti += TS)
+                for (int tc = 0; tc < 128 && tj + tc < n2; tc += TS)
+                    update_tile<T, NB>(A, lda, k0, mrows, kb + ti, kb + tj + tc, S.P, S.u.Bt, 128, tc, vec, lim);
             __syncthreads();
         }
     }
@@ -824,28 +718,10 @@ __device__ int cta_chol_factor(T *__restrict__ A, int lda, int n, CtaSmem<T> &S,
         }
         // A22 -= L21 L21^T on the lower triangle; both operands come from the panel.
         auto lim = [&](int r, int c) { return min(mrows, r + 1) - c; };
-        bool done = false;
-        if constexpr (CtaStage<T>::value > 1) {
-            if (vec) {
-                const int nt = (m2 + 63) / 64;
-                update_tiles_staged<NB>(A, lda, k0, mrows, nt * (nt + 1) / 2,
-                                        [&](int t, int &r0, int &c0, int &b0) {
-                                            int ti = 0;
-                                            while ((ti + 1) * (ti + 2) / 2 <= t) ti++;
-                                            r0 = kb + ti * 64;
-                                            c0 = kb + (t - ti * (ti + 1) / 2) * 64;
-                                            b0 = c0;
-                                        },
-                                        S.P, S.P, CTA_LDP, lim, S.Cst, false);
-                done = true;
-            }
-        }
-        if (!done) {
-            constexpr int TS = TileCfg<T>::TS;
-            for (int ti = 0; ti < m2; ti += TS)
-                for (int tj = 0; tj <= ti; tj += TS)
-                    update_tile<T, NB>(A, lda, k0, mrows, kb + ti, kb + tj, S.P, S.P, CTA_LDP, kb + tj, vec, lim);
-        }
+        constexpr int TS = TileCfg<T>::TS;
+        for (int ti = 0; ti < m2; ti += TS)
+            for (int tj = 0; tj <= ti; tj += TS)
+                update_tile<T, NB>(A, lda, k0, mrows, kb + ti, kb + tj, S.P, S.P, CTA_LDP, kb + tj, vec, lim);
         __syncthreads();
     }
     return RL_OK;

@@ -123,6 +123,7 @@ void finish(rl_server &s, Req *q, rl_status st) {
 // ------------------------------------------------------------------ worker jobs --
 struct Worker {
     rl_server *s = nullptr;
+    int index = 0;
     cudaStream_t stream = nullptr;
     void *work32 = nullptr, *work64 = nullptr;  // batched-kernel slots
     int grid32 = 0, grid64 = 0;
@@ -327,15 +328,35 @@ struct Worker {
         return RL_OK;
     }
 
+    // Worker 0 is the fast lane: it takes only batchable (small) requests, so they never
+    // queue behind a large factorisation. The other workers take the oldest large
+    // request, or the batchable ones when no large request waits.
+    bool fast_lane() const { return index == 0 && s->cfg.workers > 1; }
+    bool has_work() const {
+        if (!fast_lane()) return !s->ready.empty();
+        for (const Req *q : s->ready)
+            if (q->batchable) return true;
+        return false;
+    }
+
     void loop() {
         for (;;) {
             std::vector<Req *> job;
             {
                 std::unique_lock<std::mutex> lk(s->mu);
-                s->cv_work.wait(lk, [&] { return s->stop || !s->ready.empty(); });
-                if (s->stop && s->ready.empty()) return;
-                Req *head = s->ready.front();
-                if (head->batchable) {
+                s->cv_work.wait(lk, [&] { return s->stop || has_work(); });
+                if (s->stop && !has_work()) return;
+                Req *head = nullptr;
+                if (!fast_lane())
+                    for (auto it = s->ready.begin(); it != s->ready.end(); ++it)
+                        if (!(*it)->batchable) {
+                            head = *it;
+                            s->ready.erase(it);
+                            break;
+                        }
+                if (head) {
+                    job.push_back(head);
+                } else {
                     for (auto it = s->ready.begin(); it != s->ready.end() && (int)job.size() < s->cfg.max_batch;) {
                         if ((*it)->batchable) {
                             job.push_back(*it);
@@ -344,9 +365,7 @@ struct Worker {
                             ++it;
                         }
                     }
-                } else {
-                    job.push_back(head);
-                    s->ready.pop_front();
+                    head = job.front();
                 }
                 const double t = now_us();
                 for (Req *q : job) q->t_start = t;
@@ -386,7 +405,7 @@ rl_status rl_server_create(const rl_server_config *cfg, rl_server **out) {
     RL_TRY(ensure_device());
     auto *s = new rl_server();
     if (cfg) s->cfg = *cfg;
-    if (s->cfg.workers <= 0) s->cfg.workers = 4;
+    if (s->cfg.workers <= 0) s->cfg.workers = 8;
     if (s->cfg.max_batch <= 0) s->cfg.max_batch = 4096;
     if (s->cfg.small_n <= 0 || s->cfg.small_n > CTA_NMAX) s->cfg.small_n = CTA_NMAX;
     size_t free_b = 0, total_b = 0;
@@ -395,8 +414,10 @@ rl_status rl_server_create(const rl_server_config *cfg, rl_server **out) {
         return RL_ERR_CUDA;
     }
     std::vector<Worker> *ws = new std::vector<Worker>(s->cfg.workers);
-    for (auto &w : *ws) {
+    for (size_t i = 0; i < ws->size(); i++) {
+        Worker &w = (*ws)[i];
         w.s = s;
+        w.index = (int)i;
         rl_status st = w.init();
         if (st != RL_OK) {
             for (auto &x : *ws) x.destroy();
