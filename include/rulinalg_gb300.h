@@ -220,8 +220,8 @@ RL_API rl_status rl_dsolve_fp64_dev(size_t n, size_t nrhs, int kind, const doubl
  * f64 result of HouseholderQr::decompose(a) and the composition Q^T b, R x = (Q^T b)[0:n]
  * (qr.rs:171-275; rl_dqr_least_squares is the all-FP64 drop-in). Householder QR of the
  * FP32 copy of A, then the corrected semi-normal equations refined in FP64 until the
- * correction is below 4u ||x||; no convergence in ten steps (or a correction that does
- * not halve) falls back to FP64 QR. info->berr is ||A^T r|| / (||A|| (||A|| ||x|| +
+ * correction is below 4u ||x|| (or stalls below 1e3 u ||x||, the floor left by the FP64
+ * residual when b is far from range(A)); anything else falls back to FP64 QR. info->berr is ||A^T r|| / (||A|| (||A|| ||x|| +
  * ||b||)) with inf-norms. The _dev form takes device pointers and synchronises the
  * stream. */
 RL_API rl_status rl_dlstsq_mixed_dev(size_t m, size_t n, const double *a, size_t lda, const double *b, double *x,

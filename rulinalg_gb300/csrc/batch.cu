@@ -82,6 +82,7 @@ rl_status record(rl_batch_plan *p, const TI *a, const TI *b, TI *x, int *info, i
     d.berr = berr;
     d.iters_tag = 0;
     d.max_iters = 30;
+    d.warp_small = 1;  // the order is largest-cost first
     RL_LAUNCH((batch_solve_kernel<TI, TF, MIXED>), p->grid, CTA_THREADS, p->smem, s, d, a, b, x);
     if (MIXED) {
         BatchDesc f = d;
@@ -91,6 +92,7 @@ rl_status record(rl_batch_plan *p, const TI *a, const TI *b, TI *x, int *info, i
         f.next = p->d_counters + 2;
         f.work = p->d_work64;
         f.iters_tag = -1;
+        f.warp_small = 0;  // the fallback list is in arrival order
         RL_LAUNCH((batch_solve_kernel<TI, double, false>), p->grid64, CTA_THREADS, p->smem64, s, f, a, b, x);
     }
     return RL_OK;
@@ -151,6 +153,7 @@ rl_status launch_chunk(rl_batch_plan *p, int c, const TI *a, const TI *b, TI *x,
     d.berr = p->h_berr;
     d.iters_tag = 0;
     d.max_iters = 30;
+    d.warp_small = 1;  // the order is largest-cost first
     RL_LAUNCH((batch_solve_kernel<TI, TF, MIXED>), std::min(p->grid, cnt), CTA_THREADS, p->smem, s, d, a, b, x);
     if (MIXED) {
         BatchDesc f = d;
@@ -160,6 +163,7 @@ rl_status launch_chunk(rl_batch_plan *p, int c, const TI *a, const TI *b, TI *x,
         f.next = ctr + 2;
         f.work = p->d_work64;
         f.iters_tag = -1;
+        f.warp_small = 0;  // the fallback list is in arrival order
         RL_LAUNCH((batch_solve_kernel<TI, double, false>), std::min(p->grid64, cnt), CTA_THREADS, p->smem64, s, f, a,
                   b, x);
     }

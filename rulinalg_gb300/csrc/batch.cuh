@@ -27,9 +27,21 @@ struct BatchDesc {
     double *berr;            // normwise backward error ||b - Ax|| / (||A|| ||x|| + ||b||), inf-norms
     int iters_tag;           // value written to iters by a plain pass (0, or -1 for fallback)
     int max_iters;           // refinement limit (mixed)
+    int warp_small;          // 1: `order` is largest-cost first (n^3, x2 for LU), so the
+                             // small tail may go to the warp-per-system path
 };
 
+// Systems of cost n^3 (x2 for LU) at most this go one per warp: a Cholesky n <= 32 or an
+// LU n <= 25, so that everything after such a system in a largest-first order fits a warp.
+constexpr double kWarpCost = 32.0 * 32.0 * 32.0;
+
 constexpr double kU64 = 1.1102230246251565e-16;  // 2^-53
+
+}  // namespace rl
+
+#include "warp_small.cuh"
+
+namespace rl {
 
 template <class TI, class TF>
 __device__ void store_solution(const BatchDesc &d, int sys, int n, TI *xi, CtaSmem<TF> &S, int st, int iters,
@@ -153,7 +165,32 @@ __global__ void __launch_bounds__(CTA_THREADS, CtaOcc<TF>::value) batch_solve_ke
         __syncthreads();
         const int it = S.item;
         __syncthreads();
-        if (it >= count) break;
+        if (it >= count) return;
+        const int sys0 = d.order[it], n0 = d.n[sys0];
+        const bool small = (double)n0 * n0 * n0 * (d.kind[sys0] ? 1.0 : 2.0) <= kWarpCost;
+        if (small && !d.warp_small) {
+            // an unordered list (the fallback pass): the small system still takes the
+            // warp path, so its arithmetic is the same in every pass
+            if (threadIdx.x < 32) warp_solve_small<TI, TF, MIXED>(d, sys0, A, B, X, S.P);
+            __syncthreads();
+            continue;
+        }
+        if (small) {
+            // Largest first: everything left is this small. From here each warp takes its
+            // own systems (warp 0 starts with this one); no CTA barrier follows.
+            const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+            TF *tile = S.P + warp * WARP_NMAX * WARP_LDT;
+            int item = warp == 0 ? it : -1;
+            for (;;) {
+                if (item < 0) {
+                    if (lane == 0) item = atomicAdd(d.next, 1);
+                    item = __shfl_sync(0xffffffffu, item, 0);
+                }
+                if (item >= count) return;
+                warp_solve_small<TI, TF, MIXED>(d, d.order[item], A, B, X, tile);
+                item = -1;
+            }
+        }
         batch_solve_one<TI, TF, MIXED>(d, d.order[it], A, B, X, W, S);
     }
 }

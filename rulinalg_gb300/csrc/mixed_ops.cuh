@@ -507,9 +507,10 @@ struct GemvT {
 // Least squares in mixed precision: Householder QR of the FP32 copy of A gives R with
 // R^T R ~ A^T A; the corrected semi-normal equations refine in FP64,
 //   r = b - A x,  g = A^T r,  x += (R^T R)^-1 g   (R solves in FP32, g scaled),
-// until the correction is below 4u ||x|| (converged to working precision). A correction
-// that does not halve, a pivot of R below FLT_MIN, or ten steps without convergence send
-// the problem to FP64 QR instead. berr reports ||A^T r|| / (||A|| (||A|| ||x|| + ||b||)),
+// until the correction is below 4u ||x|| (converged to working precision), or stalls
+// below 1e3 u ||x|| (the floor the FP64 residual leaves when b is far from range(A)).
+// A correction that stalls higher, a pivot of R below FLT_MIN, or ten steps without
+// convergence send the problem to FP64 QR instead. berr reports ||A^T r|| / (||A|| (||A|| ||x|| + ||b||)),
 // inf-norms, for the returned x.
 inline rl_status lstsq_mixed(const double *A, long long lda, int m, int n, const double *b, double *x, SolveOut &out,
                              cudaStream_t s) {
@@ -571,7 +572,13 @@ inline rl_status lstsq_mixed(const double *A, long long lda, int m, int n, const
             ok = true;
             break;
         }
-        if (it >= 1 && dn > 0.5 * prev) break;
+        if (it >= 1 && dn > 0.5 * prev) {
+            // Stalled. With a large residual b - Ax the FP64 evaluation of A^T r leaves a
+            // correction floor of about kappa^2 u ||x||: a floor this low is converged,
+            // anything above it is left to FP64 QR.
+            ok = dn <= 1e3 * kU * xn;
+            break;
+        }
         prev = dn;
     }
     if (!ok) {

@@ -113,6 +113,7 @@ extern "C" rl_status rl_dsolve_mixed_noalloc_dev(size_t n, int kind, const doubl
     d.berr = berr;
     d.iters_tag = 0;
     d.max_iters = 30;
+    d.warp_small = 1;  // the order is largest-cost first
     RL_LAUNCH((batch_solve_kernel<double, float, true>), 1, CTA_THREADS, cta_smem_bytes<float>(), st, d, a, b, x);
 
     BatchDesc f = d;
@@ -122,6 +123,7 @@ extern "C" rl_status rl_dsolve_mixed_noalloc_dev(size_t n, int kind, const doubl
     f.next = &s->counters[2];
     f.work = s->factor64;
     f.iters_tag = -1;
+    f.warp_small = 0;  // the fallback list is in arrival order
     RL_LAUNCH((batch_solve_kernel<double, double, false>), 1, CTA_THREADS, cta_smem_bytes<double>(), st, f, a, b, x);
     return RL_OK;
 }

@@ -219,6 +219,7 @@ struct Worker {
         d.berr = dberr.p;
         d.iters_tag = 0;
         d.max_iters = 30;
+        d.warp_small = 1;  // the order is largest-cost first
         RL_LAUNCH((batch_solve_kernel<double, float, true>), std::min(grid32, B), CTA_THREADS, smem32, st, d, dA.p,
                   dB.p, dX.p);
         BatchDesc f = d;
@@ -228,6 +229,7 @@ struct Worker {
         f.next = dcnt.p + 2;
         f.work = work64;
         f.iters_tag = -1;
+        f.warp_small = 0;  // the fallback list is in arrival order
         RL_LAUNCH((batch_solve_kernel<double, double, false>), std::min(grid64, B), CTA_THREADS, smem64, st, f, dA.p,
                   dB.p, dX.p);
         std::vector<int> info(B), iters(B);

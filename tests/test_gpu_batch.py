@@ -65,6 +65,32 @@ def test_batch_edge_sizes(gpu, precision):
     plan.close()
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_warp_tail_boundary(gpu, precision):
+    """The small tail of a largest-first batch (cost n^3, x2 for LU, at most 32^3) runs
+    one system per warp; systems just above the boundary (LU 26..32, Cholesky 33..40)
+    sort in between and stay on the one-CTA path. All agree with the oracle."""
+    rng = np.random.default_rng(11)
+    sizes = [32, 40, 26, 25, 32, 33, 24, 31, 2, 1, 17, 25, 26, 32, 40, 5]
+    kinds = [0, 1, 0, 0, 1, 1, 1, 0, 0, 1, 1, 1, 0, 1, 1, 0]
+    mats, rhs = make_batch(rng, sizes, kinds)
+    prec = gpu.PREC_FP64 if precision == "fp64" else gpu.PREC_MIXED
+    plan = gpu.BatchPlan(sizes, kinds, prec)
+    a, b = plan.pack(mats, rhs)
+    x, info, iters, berr = plan.solve(a, b)
+    assert (info == 0).all(), info
+    xs = plan.unpack(x)
+    for i, (m, r, k) in enumerate(zip(mats, rhs, kinds)):
+        n = sizes[i]
+        assert backward_error(m, xs[i], r) <= n * U64 * 10, (n, k)
+        assert 0 <= berr[i] <= n * U64 * 10
+        xo, st = oracle_solve(m, r, k)
+        assert np.max(np.abs(xs[i] - xo)) <= 1e-12 * max(np.max(np.abs(xo)), 1e-300) * n, (n, k)
+        if precision == "mixed":
+            assert iters[i] >= 1
+    plan.close()
+
+
 def test_batch_f32(gpu):
     rng = np.random.default_rng(9)
     sizes = EDGE_SIZES

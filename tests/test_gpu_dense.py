@@ -325,3 +325,18 @@ def test_least_squares(gpu, m, n):
     assert np.max(np.abs(x - xo)) <= 1e-10 * max(np.max(np.abs(xo)), 1)
     # optimality: A^T (A x - b) ~ 0
     assert np.linalg.norm(a.T @ (a @ x - b)) <= 1e-10 * np.linalg.norm(a) ** 2 * np.linalg.norm(x)
+
+
+@pytest.mark.parametrize("m,n", [(600, 300), (2100, 700)])
+def test_qr_f32_against_f64_oracle(gpu, m, n):
+    """The FP32 Householder QR (the mixed least-squares factor) agrees with the f64
+    oracle to FP32 accuracy; tall panels run on one thread-block cluster."""
+    rng = np.random.default_rng(m + 7 * n)
+    a = rng.standard_normal((m, n))
+    oqr, otau = O.qr_decompose(a)
+    h = gpu.HouseholderQr.decompose(a.astype(np.float32))
+    assert h.qr.dtype == np.float32
+    eps32 = 2.0 ** -24
+    assert np.max(np.abs(h.tau.astype(np.float64) - otau)) <= 50 * n * eps32
+    r32 = np.triu(h.qr.astype(np.float64))[:n]
+    assert fro(r32 - np.triu(oqr)[:n]) <= 10 * n * eps32 * fro(a)
