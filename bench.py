@@ -545,14 +545,29 @@ def main():
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     alg_bytes = a_bytes + 2 * b_bytes
+    # DRAM traffic per launch from the committed ncu summary of this kernel (captured on a
+    # 6,000-system batch of the same mix and scaled there to 40,000 by matrix bytes);
+    # scaled here by matrix bytes to this run's batch.
+    traffic = None
+    prof = ROOT / "profiles" / "batch_solve_kernel_mixed_40k_mix.md"
+    if prof.exists():
+        for line in prof.read_text().splitlines():
+            if line.startswith("traffic_per_launch_bytes:"):
+                traffic = float(line.split(":")[1]) * a_bytes / 10.0127e9
+    fp64_peak = 1.25  # TFLOP/s: rl_dgemm_dev sustains this on GB300 (bench.py --workload dense)
+    fp64_floor_ms = fl64 / (fp64_peak * 1e12) * 1e3
     roofline = {"bound": "hbm", "achieved": alg_bytes / t_k / 1e9, "peak": hbm_peak, "unit": "GB/s",
-                "frac": alg_bytes / t_k / 1e9 / hbm_peak, "traffic": None,
+                "frac": alg_bytes / t_k / 1e9 / hbm_peak, "traffic": traffic,
+                "traffic_rate_gbs": traffic / t_k / 1e9 if traffic else None,
                 "kernel": "batch_solve_kernel<double,float,true> (graph: memset + main pass + FP64 fallback pass)",
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6.8 TB/s",
                 "compute": {"fp32_tflops": fl32 / t_k / 1e12, "fp32_peak_tflops_measured": 74.26,
-                            "fp64_tflops": fl64 / t_k / 1e12, "fp64_peak_tflops_measured": 1.05,
-                            "note": "the kernel is bound by the FP32 SIMT pipe (factor) and the FP64 pipe "
-                                    "(residuals); peaks measured by a DFMA/DMMA/FFMA probe on this pool's GB300"}}
+                            "fp64_tflops": fl64 / t_k / 1e12, "fp64_peak_tflops": fp64_peak,
+                            "fp64_floor_ms": fp64_floor_ms, "frac_of_fp64_floor": fp64_floor_ms / ms_mixed,
+                            "note": "HBM is not the binding unit (algorithmic bytes are 1/10 of the DRAM "
+                                    "traffic, which runs at ~30% of peak); the binding throughput floor is "
+                                    "the FP64 pipe for the refinement residuals (fp64_floor_ms), the kernel "
+                                    "itself is latency-bound per CTA (profiles/)"}}
 
     cpu = None
     if rank == 0 and not args.skip_cpu:

@@ -330,15 +330,27 @@ struct Worker {
         return RL_OK;
     }
 
-    // Worker 0 is the fast lane: it takes only batchable (small) requests, so they never
-    // queue behind a large factorisation. The other workers take the oldest large
-    // request, or the batchable ones when no large request waits.
+    // Worker 0 is the fast lane: it takes batchable (small) requests, then re-solves
+    // against resident factors, never a large factorisation, so cheap requests do not
+    // queue behind one. The other workers take re-solves first (cheap), then the oldest
+    // large request, then batchable ones when nothing else waits.
     bool fast_lane() const { return index == 0 && s->cfg.workers > 1; }
     bool has_work() const {
         if (!fast_lane()) return !s->ready.empty();
         for (const Req *q : s->ready)
-            if (q->batchable) return true;
+            if (q->batchable || q->r.kind == RL_REQ_RESOLVE) return true;
         return false;
+    }
+    // Removes and returns the first ready request matching `pred`, or nullptr.
+    template <class Pred>
+    Req *take_first(Pred pred) {
+        for (auto it = s->ready.begin(); it != s->ready.end(); ++it)
+            if (pred(*it)) {
+                Req *q = *it;
+                s->ready.erase(it);
+                return q;
+            }
+        return nullptr;
     }
 
     void loop() {
@@ -348,14 +360,16 @@ struct Worker {
                 std::unique_lock<std::mutex> lk(s->mu);
                 s->cv_work.wait(lk, [&] { return s->stop || has_work(); });
                 if (s->stop && !has_work()) return;
+                auto is_resolve = [](const Req *q) { return q->r.kind == RL_REQ_RESOLVE; };
                 Req *head = nullptr;
-                if (!fast_lane())
-                    for (auto it = s->ready.begin(); it != s->ready.end(); ++it)
-                        if (!(*it)->batchable) {
-                            head = *it;
-                            s->ready.erase(it);
-                            break;
-                        }
+                if (fast_lane()) {
+                    bool any_batchable = false;
+                    for (const Req *q : s->ready) any_batchable |= q->batchable;
+                    if (!any_batchable) head = take_first(is_resolve);
+                } else {
+                    head = take_first(is_resolve);
+                    if (!head) head = take_first([](const Req *q) { return !q->batchable; });
+                }
                 if (head) {
                     job.push_back(head);
                 } else {
