@@ -8,12 +8,32 @@
 #include <vector>
 
 #include "dense_ops.cuh"
+#include "gemm_tc.cuh"
 
 namespace rl {
 
 namespace {
 
 // ------------------------------------------------------------- host entry points --
+
+// The public GEMM: FP32 with 16-byte-aligned rows and at least one 128 x 128 tile can go
+// to the tensor cores (3xTF32, FP32 accuracy); everything else to the SIMT kernel. The
+// register-staged tensor-core kernel measured 18 TFLOP/s at n = 8192 against 44 for the
+// SIMT kernel (its shared-memory stores conflict), so it stays off until its loads move
+// to TMA.
+constexpr bool kSgemmTensorCores = false;
+template <class T>
+rl_status gemm_public(int m, int n, int k, const T *a, long long lda, const T *b, long long ldb, T *c, long long ldc,
+                      cudaStream_t s, bool &used_tc) {
+    used_tc = false;
+    if constexpr (std::is_same<T, float>::value) {
+        if (kSgemmTensorCores && sgemm_tc_eligible(m, n, k, a, lda, b, ldb)) {
+            used_tc = true;
+            return sgemm_tc(m, n, k, 1.f, a, lda, b, ldb, 0.f, c, ldc, s);
+        }
+    }
+    return gemm<T, false, false>(m, n, k, T(1), a, lda, b, ldb, T(0), c, ldc, s);
+}
 
 template <class T>
 rl_status gemm_host(size_t m, size_t k, size_t n, const T *a, size_t rsa, const T *b, size_t rsb, T *c, size_t rsc) {
@@ -29,10 +49,12 @@ rl_status gemm_host(size_t m, size_t k, size_t n, const T *a, size_t rsa, const 
     RL_TRY(dC.alloc(m * n, s));
     RL_TRY(copy_h2d(dA.p, k, a, rsa, m, k, s));
     RL_TRY(copy_h2d(dB.p, n, b, rsb, k, n, s));
-    RL_TRY((gemm<T, false, false>((int)m, (int)n, (int)k, T(1), dA.p, (long long)k, dB.p, (long long)n, T(0), dC.p,
-                                  (long long)n, s)));
+    bool used_tc = false;
+    RL_TRY(gemm_public<T>((int)m, (int)n, (int)k, dA.p, (long long)k, dB.p, (long long)n, dC.p, (long long)n, s,
+                          used_tc));
     RL_TRY(copy_d2h(c, rsc, dC.p, n, m, n, s));
     RL_TRY_CUDA(cudaStreamSynchronize(s));
+    if (used_tc) RL_TRY(sgemm_tc_status(s));
     return RL_OK;
 }
 
@@ -43,8 +65,9 @@ rl_status gemm_dev(size_t m, size_t k, size_t n, const T *a, size_t rsa, const T
     if (!c || (k && (!a || !b))) return RL_ERR_INVALID_ARG;
     if (!fits_int(m) || !fits_int(n) || !fits_int(k)) return RL_ERR_INVALID_ARG;
     RL_TRY(ensure_device());
-    return gemm<T, false, false>((int)m, (int)n, (int)k, T(1), a, (long long)rsa, b, (long long)rsb, T(0), c,
-                                 (long long)rsc, resolve_stream(stream));
+    bool used_tc = false;
+    return gemm_public<T>((int)m, (int)n, (int)k, a, (long long)rsa, b, (long long)rsb, c, (long long)rsc,
+                          resolve_stream(stream), used_tc);
 }
 
 template <class T>

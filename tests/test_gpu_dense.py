@@ -59,6 +59,21 @@ def test_gemm_normwise(gpu, dtype, m, k, n):
     assert fro(got.astype(np.float64) - ref) <= max(k, 1) * eps * fro(a) * fro(b)
 
 
+@pytest.mark.parametrize("m,k,n", [(128, 32, 128), (256, 256, 256), (200, 100, 300), (130, 36, 132),
+                                   (1024, 512, 768), (2048, 2048, 2048)])
+def test_sgemm_tensor_core_elementwise(gpu, m, k, n):
+    """Shapes that take the tcgen05 3xTF32 path (rows 16-byte aligned, at least one
+    128 x 128 tile): every element within the FP32 dot-product bound 2 k eps (|A| |B|)."""
+    rng = np.random.default_rng(m + 3 * k + 7 * n)
+    a = rng.standard_normal((m, k)).astype(np.float32)
+    b = rng.standard_normal((k, n)).astype(np.float32)
+    got = gpu.mat_mul(a, b).astype(np.float64)
+    a64, b64 = a.astype(np.float64), b.astype(np.float64)
+    ref = a64 @ b64
+    bound = 2 * k * U32 * (np.abs(a64) @ np.abs(b64))
+    assert np.all(np.abs(got - ref) <= bound), np.max(np.abs(got - ref) / bound)
+
+
 def test_gemm_k_zero_and_empty(gpu):
     c = gpu.mat_mul(np.zeros((3, 0)), np.zeros((0, 4)))
     assert c.shape == (3, 4) and not c.any()
