@@ -16,18 +16,14 @@ namespace {
 
 // ------------------------------------------------------------- host entry points --
 
-// The public GEMM: FP32 with 16-byte-aligned rows and at least one 128 x 128 tile can go
-// to the tensor cores (3xTF32, FP32 accuracy); everything else to the SIMT kernel. The
-// register-staged tensor-core kernel measured 18 TFLOP/s at n = 8192 against 44 for the
-// SIMT kernel (its shared-memory stores conflict), so it stays off until its loads move
-// to TMA.
-constexpr bool kSgemmTensorCores = false;
+// The public GEMM: FP32 with at least one 128 x 128 tile (and K >= 64) runs on the
+// tensor cores (3xTF32, FP32 accuracy); everything else, and all FP64, on the SIMT kernel.
 template <class T>
 rl_status gemm_public(int m, int n, int k, const T *a, long long lda, const T *b, long long ldb, T *c, long long ldc,
                       cudaStream_t s, bool &used_tc) {
     used_tc = false;
     if constexpr (std::is_same<T, float>::value) {
-        if (kSgemmTensorCores && sgemm_tc_eligible(m, n, k, a, lda, b, ldb)) {
+        if (sgemm_tc_eligible(m, n, k)) {
             used_tc = true;
             return sgemm_tc(m, n, k, 1.f, a, lda, b, ldb, 0.f, c, ldc, s);
         }

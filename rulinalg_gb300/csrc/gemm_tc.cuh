@@ -1,62 +1,62 @@
-// FP32 GEMM on the 5th-generation tensor cores (tcgen05, TF32 inputs, FP32 accumulation
-// in tensor memory) with FP32 accuracy from the 3xTF32 split: every operand x is held as
-// hi = tf32(x) (round to nearest) and lo = x - hi, and each product as
-// a_lo b_hi + a_hi b_lo + a_hi b_hi (the a_lo b_lo term is below FP32 rounding).
+// FP32 GEMM on the 5th-generation tensor cores with FP32 accuracy (3xTF32):
 //
 //     C = alpha * A * B + beta * C,  A (m x k), B (k x n), C (m x n), row-major.
 //
-// One CTA (4 warps) computes a 128 x 128 tile of C in 128 columns of tensor memory.
-// K advances in chunks of 32: all threads load the chunk of A and B from global memory,
-// split it and store hi and lo into shared memory in the no-swizzle K-major "core
-// matrix" layout (8 rows x 16 bytes per core matrix; core matrices 128 bytes apart along
-// K and 256 bytes apart along M/N), one thread issues the 12 MMAs of the chunk
-// (4 k-steps of 8 x 3 products) and commits them to the chunk's mbarrier. Two chunk
-// buffers alternate, so the next chunk's loads overlap the current chunk's MMAs; a buffer
-// is rewritten only after its mbarrier reports the MMAs that read it complete. The
-// epilogue reads the accumulator back with tcgen05.ld (warp w owns rows 32w..32w+31).
-// Every mbarrier wait is bounded; on expiry the CTA records RL_ERR_TIMEOUT, skips the
-// epilogue, frees its tensor memory and returns.
+// Every operand x is split once into hi = tf32(x) (round to nearest) and lo = x - hi
+// (split_rows_kernel for A, split_transpose_kernel for B, which also transposes B to
+// K-major), and each product is accumulated as a_lo b_hi + a_hi b_lo + a_hi b_hi in FP32
+// in tensor memory (the a_lo b_lo term is below FP32 rounding).
+//
+// sgemm_tma_kernel: one CTA (4 warps) per 128 x 128 tile of C, accumulator in 128
+// columns of tensor memory. K advances in chunks of 32 through a 3-stage ring of shared
+// memory, each stage holding the four 128 x 32 operand tiles (A_hi, A_lo, B_hi, B_lo),
+// loaded by TMA with the 128-byte swizzle the MMA descriptors expect. Warp 0 lane 0
+// produces (waits for a stage to be empty, arms its mbarrier with the byte count, issues
+// the four tensor copies), warp 1 lane 0 issues the 12 MMAs of each chunk (4 k-steps x
+// 3 products, kind::tf32, M = N = 128, K = 8) and commits them to the stage's empty
+// barrier, and finally to a done barrier that the four warps wait on before reading the
+// accumulator back with tcgen05.ld (warp w owns rows 32w .. 32w + 31). Every mbarrier wait
+// is bounded; on expiry the CTA records RL_ERR_TIMEOUT, writes NaN over its tile, frees
+// its tensor memory and returns.
 #pragma once
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <cstdint>
+#include <mutex>
 
 #include "common.cuh"
 
 namespace rl {
 namespace tc {
 
-constexpr int BM = 128, BN = 128, BK = 32;
-constexpr int KSTEP = 8;                       // K of one kind::tf32 MMA
-constexpr int NSTEP = BK / KSTEP;              // MMA k-steps per chunk
-constexpr int OPER_BYTES = BM * KSTEP * 4;     // one operand k-step tile (128 rows x 8): 4 KB
-constexpr int CHUNK_BYTES = NSTEP * OPER_BYTES;  // one operand chunk: 16 KB
-constexpr int STAGE_BYTES = 4 * CHUNK_BYTES;   // A_hi, A_lo, B_hi, B_lo: 64 KB
-constexpr int SMEM_BYTES = 2 * STAGE_BYTES + 64;
+constexpr int BM = 128, BN = 128, BK = 32, STAGES = 3;
+constexpr int TILE_BYTES = BM * BK * 4;        // one 128 x 32 FP32 operand tile: 16 KB
+constexpr int STAGE_BYTES = 4 * TILE_BYTES;    // A_hi, A_lo, B_hi, B_lo: 64 KB
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;  // + alignment slack + barriers
 constexpr int THREADS = 128;
 constexpr int TMEM_COLS = 128;
 constexpr unsigned long long kWaitLimit = 1ull << 26;  // polls of an mbarrier before giving up
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-// Shared-memory matrix descriptor: no swizzle, K-major, leading (K) and stride (M/N)
-// byte offsets between core matrices.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+// Shared-memory matrix descriptor for a K-major operand in the 128-byte swizzle layout
+// (8-row groups 1024 bytes apart; the start address moves by 32 bytes per K = 8 step
+// inside the 128-byte swizzle atom).
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
     uint64_t d = 0;
     d |= (uint64_t)((addr >> 4) & 0x3FFFu);
-    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-    d |= (uint64_t)1 << 46;  // descriptor version of this architecture
-    return d;                // base offset 0, layout type 0 (no swizzle)
+    d |= (uint64_t)1 << 16;             // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset: 8 rows x 128 bytes
+    d |= (uint64_t)1 << 46;             // descriptor version of this architecture
+    d |= (uint64_t)2 << 61;             // layout: 128-byte swizzle
+    return d;
 }
 
 // Instruction descriptor of kind::tf32: D F32, A and B TF32, both K-major, N, M.
 __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
     return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-// Byte offset of element (row r, k) inside one 128 x 8 k-step tile.
-__device__ __forceinline__ uint32_t tile_off(int r, int k) {
-    return (uint32_t)((r >> 3) * 256 + (k >> 2) * 128 + (r & 7) * 16 + (k & 3) * 4);
 }
 
 __device__ __forceinline__ float tf32_rna(float x) {
@@ -67,6 +67,11 @@ __device__ __forceinline__ float tf32_rna(float x) {
 
 __device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
 }
 
 // Bounded wait for the given phase parity; false on expiry.
@@ -84,6 +89,15 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
         if (done) return true;
     }
     return false;
+}
+
+// 2D tensor copy global -> shared (x = the K coordinate, y = the row), completing on bar.
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
 }
 
 __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
@@ -115,17 +129,61 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 
 }  // namespace tc
 
-// A and B rows must start 16-byte aligned (lda, ldb multiples of 4, A and B aligned).
+// hi/lo of A (rows x k, row stride ldx) into rows x kp buffers (kp = k rounded up to 32,
+// zero beyond k).
+static __global__ void split_rows_kernel(const float *__restrict__ X, long long ldx, int rows, int k, int kp,
+                                         float *__restrict__ hi, float *__restrict__ lo) {
+    const long long total = (long long)rows * kp;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const int r = (int)(e / kp), c = (int)(e - (long long)r * kp);
+        const float x = c < k ? X[(long long)r * ldx + c] : 0.f;
+        const float h = tc::tf32_rna(x);
+        hi[e] = h;
+        lo[e] = x - h;
+    }
+}
+
+// hi/lo of B^T: B is k x n (row stride ldb); outputs are n x kp (K-major), zero beyond k.
+// 32 x 32 tiles through shared memory; block (32, 8).
+static __global__ void split_transpose_kernel(const float *__restrict__ B, long long ldb, int k, int n, int kp,
+                                              float *__restrict__ hi, float *__restrict__ lo) {
+    __shared__ float t[32][33];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int n0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const int kk = k0 + ty + 8 * j, nn = n0 + tx;
+        t[ty + 8 * j][tx] = (kk < k && nn < n) ? B[(long long)kk * ldb + nn] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const int nn = n0 + ty + 8 * j, kk = k0 + tx;
+        if (nn < n) {
+            const float x = t[tx][ty + 8 * j];
+            const float h = tc::tf32_rna(x);
+            hi[(long long)nn * kp + kk] = h;
+            lo[(long long)nn * kp + kk] = x - h;
+        }
+    }
+}
+
 static __global__ void __launch_bounds__(tc::THREADS, 1)
-    sgemm_tc_kernel(int m, int n, int k, float alpha, const float *__restrict__ A, long long lda,
-                    const float *__restrict__ B, long long ldb, float beta, float *__restrict__ C, long long ldc,
-                    int *err) {
+    sgemm_tma_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUtensorMap tAl,
+                     const __grid_constant__ CUtensorMap tBh, const __grid_constant__ CUtensorMap tBl, int m, int n,
+                     int kp, float alpha, float beta, float *__restrict__ C, long long ldc, int *err) {
     using namespace tc;
-    extern __shared__ __align__(1024) unsigned char smem[];
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + 2 * STAGE_BYTES);  // 2 mbarriers
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + 2 * STAGE_BYTES + 16);
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char *smem =
+        reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + STAGES * STAGE_BYTES);
+    uint64_t *empty = full + STAGES;
+    uint64_t *done = empty + STAGES;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+    __shared__ int s_fail;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int row0 = blockIdx.y * BM, col0 = blockIdx.x * BN;
+    const int nk = kp / BK;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
@@ -134,148 +192,151 @@ static __global__ void __launch_bounds__(tc::THREADS, 1)
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+        s_fail = 0;
+        for (int s = 0; s < STAGES; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
-    constexpr uint32_t idesc = idesc_tf32(BM, BN);
-    bool ok = true;
 
-    const int nchunks = (k + BK - 1) / BK;
-    for (int c = 0; c < nchunks && ok; c++) {
-        const int s = c & 1;
-        unsigned char *st = smem + s * STAGE_BYTES;
-        if (c >= 2) ok = mbar_wait(&bar[s], ((c - 2) >> 1) & 1);  // the MMAs that read this stage
-        if (!__syncthreads_and(ok)) {
-            ok = false;
-            break;
-        }
-        const int k0 = c * BK;
-        // A chunk: 128 rows x 32 k, float4 along k (one core-matrix row per float4)
-#pragma unroll
-        for (int e = 0; e < (BM * BK / 4) / THREADS; e++) {
-            const int idx = tid + e * THREADS, r = idx >> 3, kq = (idx & 7) * 4;
-            const int gr = row0 + r, gk = k0 + kq;
-            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (gr < m) {
-                const float *src = A + (long long)gr * lda + gk;
-                if (gk + 3 < k)
-                    v = *reinterpret_cast<const float4 *>(src);
-                else {
-                    if (gk < k) v.x = src[0];
-                    if (gk + 1 < k) v.y = src[1];
-                    if (gk + 2 < k) v.z = src[2];
-                }
+    if (warp == 0 && lane == 0) {  // producer
+        for (int c = 0; c < nk; c++) {
+            const int s = c % STAGES, use = c / STAGES;
+            if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1)) {
+                s_fail = 1;
+                break;
             }
-            const float h0 = tf32_rna(v.x), h1 = tf32_rna(v.y), h2 = tf32_rna(v.z), h3 = tf32_rna(v.w);
-            const uint32_t off = (kq >> 3) * OPER_BYTES + tile_off(r, kq & 7);
-            *reinterpret_cast<float4 *>(st + off) = make_float4(h0, h1, h2, h3);
-            *reinterpret_cast<float4 *>(st + CHUNK_BYTES + off) =
-                make_float4(v.x - h0, v.y - h1, v.z - h2, v.w - h3);
+            unsigned char *st = smem + s * STAGE_BYTES;
+            mbar_expect_tx(&full[s], STAGE_BYTES);
+            tma_load_2d(st, &tAh, c * BK, row0, &full[s]);
+            tma_load_2d(st + TILE_BYTES, &tAl, c * BK, row0, &full[s]);
+            tma_load_2d(st + 2 * TILE_BYTES, &tBh, c * BK, col0, &full[s]);
+            tma_load_2d(st + 3 * TILE_BYTES, &tBl, c * BK, col0, &full[s]);
         }
-        // B chunk: 32 k x 128 n, float4 along n (four rows of the K-major B tile)
-#pragma unroll
-        for (int e = 0; e < (BK * BN / 4) / THREADS; e++) {
-            const int idx = tid + e * THREADS, kk = idx >> 5, nq = (idx & 31) * 4;
-            const int gk = k0 + kk, gn = col0 + nq;
-            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (gk < k) {
-                const float *src = B + (long long)gk * ldb + gn;
-                if (gn + 3 < n)
-                    v = *reinterpret_cast<const float4 *>(src);
-                else {
-                    if (gn < n) v.x = src[0];
-                    if (gn + 1 < n) v.y = src[1];
-                    if (gn + 2 < n) v.z = src[2];
-                }
+    } else if (warp == 1 && lane == 0) {  // MMA issuer
+        constexpr uint32_t idesc = idesc_tf32(BM, BN);
+        for (int c = 0; c < nk; c++) {
+            const int s = c % STAGES, use = c / STAGES;
+            if (!mbar_wait(&full[s], use & 1)) {
+                s_fail = 1;
+                break;
             }
-            const float x[4] = {v.x, v.y, v.z, v.w};
-            unsigned char *bh = st + 2 * CHUNK_BYTES + (kk >> 3) * OPER_BYTES;
-            unsigned char *bl = st + 3 * CHUNK_BYTES + (kk >> 3) * OPER_BYTES;
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const float h = tf32_rna(x[q]);
-                const uint32_t off = tile_off(nq + q, kk & 7);
-                *reinterpret_cast<float *>(bh + off) = h;
-                *reinterpret_cast<float *>(bl + off) = x[q] - h;
-            }
-        }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // make the stores visible to the MMAs
-        __syncthreads();
-        if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t base = smem_u32(st);
+            const uint32_t base = smem_u32(smem + s * STAGE_BYTES);
 #pragma unroll
-            for (int ks = 0; ks < NSTEP; ks++) {
-                const uint32_t o = ks * OPER_BYTES;
-                const uint64_t ah = smem_desc(base + o, 128, 256), al = smem_desc(base + CHUNK_BYTES + o, 128, 256);
-                const uint64_t bh = smem_desc(base + 2 * CHUNK_BYTES + o, 128, 256),
-                               bl = smem_desc(base + 3 * CHUNK_BYTES + o, 128, 256);
+            for (int ks = 0; ks < BK / 8; ks++) {
+                const uint32_t o = ks * 32;
+                const uint64_t ah = smem_desc_sw128(base + o), al = smem_desc_sw128(base + TILE_BYTES + o);
+                const uint64_t bh = smem_desc_sw128(base + 2 * TILE_BYTES + o),
+                               bl = smem_desc_sw128(base + 3 * TILE_BYTES + o);
                 mma_tf32(tmem, al, bh, idesc, (c > 0 || ks > 0) ? 1u : 0u);
                 mma_tf32(tmem, ah, bl, idesc, 1u);
                 mma_tf32(tmem, ah, bh, idesc, 1u);
             }
-            mma_commit(&bar[s]);
+            mma_commit(&empty[s]);
         }
+        mma_commit(done);
     }
-    // all MMAs done: the last chunk's commit covers every earlier MMA of this thread
-    if (ok && nchunks > 0) ok = mbar_wait(&bar[(nchunks - 1) & 1], ((nchunks - 1) >> 1) & 1);
-    ok = __syncthreads_and(ok) != 0;
+    __syncwarp();
+    bool ok = nk == 0 || mbar_wait(done, 0);
+    ok = __syncthreads_and(ok && !s_fail) != 0;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (ok) {
-        const int r = row0 + warp * 32 + lane;
+    const int r = row0 + warp * 32 + lane;
 #pragma unroll 1
-        for (int c0 = 0; c0 < BN; c0 += 16) {
-            float v[16];
+    for (int c0 = 0; c0 < BN; c0 += 16) {
+        float v[16];
+        if (ok && nk > 0) {
             tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-            if (r < m) {
-                float *dst = C + (long long)r * ldc + col0 + c0;
+        } else {
 #pragma unroll
-                for (int j = 0; j < 16; j++) {
-                    if (col0 + c0 + j < n) {
-                        float out = alpha * (nchunks > 0 ? v[j] : 0.f);
-                        if (beta != 0.f) out = fmaf(beta, dst[j], out);
-                        dst[j] = out;
-                    }
+            for (int j = 0; j < 16; j++) v[j] = ok ? 0.f : __int_as_float(0x7fc00000);
+        }
+        if (r < m) {
+            float *dst = C + (long long)r * ldc + col0 + c0;
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+                if (col0 + c0 + j < n) {
+                    float out = alpha * v[j];
+                    if (ok && beta != 0.f) out = fmaf(beta, dst[j], out);
+                    dst[j] = out;
                 }
             }
         }
-    } else if (tid == 0) {
-        atomicCAS(err, 0, RL_ERR_TIMEOUT);
     }
+    if (!ok && tid == 0) atomicCAS(err, 0, RL_ERR_TIMEOUT);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
 }
 
-}  // namespace rl
-
-namespace rl {
-
 // Sticky timeout word of the tensor-core GEMM (one per translation unit that launches it).
 static __device__ int g_sgemm_tc_err;
 
-inline bool sgemm_tc_eligible(int m, int n, int k, const float *A, long long lda, const float *B, long long ldb) {
-    return m >= 128 && n >= 128 && k >= tc::BK && lda % 4 == 0 && ldb % 4 == 0 &&
-           reinterpret_cast<uintptr_t>(A) % 16 == 0 && reinterpret_cast<uintptr_t>(B) % 16 == 0;
+inline bool sgemm_tc_eligible(int m, int n, int k) { return m >= 128 && n >= 128 && k >= 64; }
+
+// cuTensorMapEncodeTiled from the driver, looked up once.
+inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        cudaGetLastError();
+    });
+    return fn;
 }
 
-// C = alpha A B + beta C on the tensor cores (3xTF32); the caller checks eligibility.
+// A rows x kp FP32 matrix (row stride kp) as 128 x 32 tiles with the 128-byte swizzle.
+inline rl_status make_tile_map(CUtensorMap &map, const float *base, int rows, int kp) {
+    auto enc = tensor_map_encoder();
+    if (!enc) return RL_ERR_CUDA;
+    const cuuint64_t dims[2] = {(cuuint64_t)kp, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)kp * sizeof(float)};
+    const cuuint32_t box[2] = {(cuuint32_t)tc::BK, (cuuint32_t)tc::BM};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(base), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? RL_OK : RL_ERR_CUDA;
+}
+
+// C = alpha A B + beta C on the tensor cores (3xTF32); any strides, any alignment.
 inline rl_status sgemm_tc(int m, int n, int k, float alpha, const float *A, long long lda, const float *B, long long ldb,
                           float beta, float *C, long long ldc, cudaStream_t s) {
     static const cudaError_t attr =
-        cudaFuncSetAttribute(sgemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
+        cudaFuncSetAttribute(sgemm_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
     RL_TRY_CUDA(attr);
+    const int kp = (k + tc::BK - 1) / tc::BK * tc::BK;
+    DevBuf<float> Ah, Al, Bh, Bl;
+    RL_TRY(Ah.alloc((size_t)m * kp, s));
+    RL_TRY(Al.alloc((size_t)m * kp, s));
+    RL_TRY(Bh.alloc((size_t)n * kp, s));
+    RL_TRY(Bl.alloc((size_t)n * kp, s));
+    const long long ta = (long long)m * kp;
+    RL_LAUNCH(split_rows_kernel, (int)std::min<long long>(8LL * num_sms(), (ta + 255) / 256), 256, 0, s, A, lda, m, k,
+              kp, Ah.p, Al.p);
+    RL_LAUNCH(split_transpose_kernel, dim3((n + 31) / 32, kp / 32), dim3(32, 8), 0, s, B, ldb, k, n, kp, Bh.p, Bl.p);
+    CUtensorMap mAh, mAl, mBh, mBl;
+    RL_TRY(make_tile_map(mAh, Ah.p, m, kp));
+    RL_TRY(make_tile_map(mAl, Al.p, m, kp));
+    RL_TRY(make_tile_map(mBh, Bh.p, n, kp));
+    RL_TRY(make_tile_map(mBl, Bl.p, n, kp));
     int *err = nullptr;
     RL_TRY_CUDA(cudaGetSymbolAddress(reinterpret_cast<void **>(&err), g_sgemm_tc_err));
     const dim3 grid((n + tc::BN - 1) / tc::BN, (m + tc::BM - 1) / tc::BM);
-    RL_LAUNCH(sgemm_tc_kernel, grid, tc::THREADS, tc::SMEM_BYTES, s, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc,
-              err);
+    RL_LAUNCH(sgemm_tma_kernel, grid, tc::THREADS, tc::SMEM_BYTES, s, mAh, mAl, mBh, mBl, m, n, kp, alpha, beta, C,
+              ldc, err);
     return RL_OK;
 }
 
