@@ -25,7 +25,7 @@ rl_status gemm_public(int m, int n, int k, const T *a, long long lda, const T *b
     if constexpr (std::is_same<T, float>::value) {
         if (sgemm_tc_eligible(m, n, k)) {
             used_tc = true;
-            return sgemm_tc(m, n, k, 1.f, a, lda, b, ldb, 0.f, c, ldc, s);
+            return sgemm_tc<false, false>(m, n, k, 1.f, a, lda, b, ldb, 0.f, c, ldc, false, s);
         }
     }
     return gemm<T, false, false>(m, n, k, T(1), a, lda, b, ldb, T(0), c, ldc, s);

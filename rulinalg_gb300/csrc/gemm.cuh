@@ -8,7 +8,10 @@
 // conflict-free.
 #pragma once
 
+#include <type_traits>
+
 #include "common.cuh"
+#include "gemm_tc.cuh"
 
 namespace rl {
 
@@ -183,11 +186,16 @@ __global__ void __launch_bounds__((GemmCfg<T>::BM / GemmCfg<T>::TM) * (GemmCfg<T
     }
 }
 
-// Launches C = alpha * op(A) op(B) + beta * C on `stream`.
+// Launches C = alpha * op(A) op(B) + beta * C on `stream`. FP32 products with at least
+// a 128 x 128 tile's worth of C and K >= 256 go to the tcgen05 kernel (gemm_tc.cuh).
 template <class T, bool TA, bool TB, bool LOWER = false>
 rl_status gemm(int m, int n, int k, T alpha, const T *A, long long lda, const T *B, long long ldb, T beta, T *C,
                long long ldc, cudaStream_t stream) {
     if (m <= 0 || n <= 0) return RL_OK;
+    if constexpr (std::is_same<T, float>::value) {  // FP32 with enough work: tensor cores (3xTF32)
+        if (sgemm_tc_eligible(m, n, k))
+            return sgemm_tc<TA, TB>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, LOWER, stream);
+    }
     constexpr int BM = GemmCfg<T>::BM, BN = GemmCfg<T>::BN;
     constexpr int NT = (BM / GemmCfg<T>::TM) * (BN / GemmCfg<T>::TN);
     dim3 grid((n + BN - 1) / BN, (m + BM - 1) / BM);

@@ -171,8 +171,11 @@ static __global__ void split_transpose_kernel(const float *__restrict__ B, long 
 static __global__ void __launch_bounds__(tc::THREADS, 1)
     sgemm_tma_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUtensorMap tAl,
                      const __grid_constant__ CUtensorMap tBh, const __grid_constant__ CUtensorMap tBl, int m, int n,
-                     int kp, float alpha, float beta, float *__restrict__ C, long long ldc, int *err) {
+                     int kp, float alpha, float beta, float *__restrict__ C, long long ldc, int lower, int *err) {
     using namespace tc;
+    // lower: only the elements on or below the diagonal are written (the SYRK form);
+    // tiles wholly above it do nothing
+    if (lower && (int)(blockIdx.x * BN) >= (int)(blockIdx.y * BM) + BM) return;
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem =
         reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -261,7 +264,7 @@ static __global__ void __launch_bounds__(tc::THREADS, 1)
             float *dst = C + (long long)r * ldc + col0 + c0;
 #pragma unroll
             for (int j = 0; j < 16; j++) {
-                if (col0 + c0 + j < n) {
+                if (col0 + c0 + j < n && !(lower && col0 + c0 + j > r)) {
                     float out = alpha * v[j];
                     if (ok && beta != 0.f) out = fmaf(beta, dst[j], out);
                     dst[j] = out;
@@ -279,7 +282,13 @@ static __global__ void __launch_bounds__(tc::THREADS, 1)
 // Sticky timeout word of the tensor-core GEMM (one per translation unit that launches it).
 static __device__ int g_sgemm_tc_err;
 
-inline bool sgemm_tc_eligible(int m, int n, int k) { return m >= 128 && n >= 128 && k >= 64; }
+// Shapes worth the tensor cores: at least half a 128 x 128 tile of C in each direction
+// and K >= 256. Below that K the per-call split, tensor-map set-up and a pipeline that
+// never fills cost more than the SIMT kernel saves (the K = 64 trailing updates of the
+// blocked factorisations measured slower on this path).
+inline bool sgemm_tc_eligible(int m, int n, int k) {
+    return m >= 64 && n >= 64 && (long long)m * n >= 128 * 128 && k >= 256;
+}
 
 // cuTensorMapEncodeTiled from the driver, looked up once.
 inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
@@ -311,9 +320,12 @@ inline rl_status make_tile_map(CUtensorMap &map, const float *base, int rows, in
     return r == CUDA_SUCCESS ? RL_OK : RL_ERR_CUDA;
 }
 
-// C = alpha A B + beta C on the tensor cores (3xTF32); any strides, any alignment.
-inline rl_status sgemm_tc(int m, int n, int k, float alpha, const float *A, long long lda, const float *B, long long ldb,
-                          float beta, float *C, long long ldc, cudaStream_t s) {
+// C = alpha op(A) op(B) + beta C on the tensor cores (3xTF32); any strides, any
+// alignment. op(A) = A (m x k, A[i * lda + p]) or A^T (A[p * lda + i]); op(B) = B (k x n,
+// B[p * ldb + j]) or B^T (B[j * ldb + p]). The split kernels repack both operands K-major.
+template <bool TA, bool TB>
+rl_status sgemm_tc(int m, int n, int k, float alpha, const float *A, long long lda, const float *B, long long ldb,
+                   float beta, float *C, long long ldc, bool lower, cudaStream_t s) {
     static const cudaError_t attr =
         cudaFuncSetAttribute(sgemm_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
     RL_TRY_CUDA(attr);
@@ -323,10 +335,19 @@ inline rl_status sgemm_tc(int m, int n, int k, float alpha, const float *A, long
     RL_TRY(Al.alloc((size_t)m * kp, s));
     RL_TRY(Bh.alloc((size_t)n * kp, s));
     RL_TRY(Bl.alloc((size_t)n * kp, s));
-    const long long ta = (long long)m * kp;
-    RL_LAUNCH(split_rows_kernel, (int)std::min<long long>(8LL * num_sms(), (ta + 255) / 256), 256, 0, s, A, lda, m, k,
-              kp, Ah.p, Al.p);
-    RL_LAUNCH(split_transpose_kernel, dim3((n + 31) / 32, kp / 32), dim3(32, 8), 0, s, B, ldb, k, n, kp, Bh.p, Bl.p);
+    auto split_rows = [&](const float *X, long long ldx, int rows, float *hi, float *lo) -> rl_status {
+        const long long t = (long long)rows * kp;
+        RL_LAUNCH(split_rows_kernel, (int)std::min<long long>(8LL * num_sms(), (t + 255) / 256), 256, 0, s, X, ldx,
+                  rows, k, kp, hi, lo);
+        return RL_OK;
+    };
+    auto split_t = [&](const float *X, long long ldx, int rows, float *hi, float *lo) -> rl_status {
+        RL_LAUNCH(split_transpose_kernel, dim3((rows + 31) / 32, kp / 32), dim3(32, 8), 0, s, X, ldx, k, rows, kp, hi,
+                  lo);
+        return RL_OK;
+    };
+    RL_TRY(TA ? split_t(A, lda, m, Ah.p, Al.p) : split_rows(A, lda, m, Ah.p, Al.p));
+    RL_TRY(TB ? split_rows(B, ldb, n, Bh.p, Bl.p) : split_t(B, ldb, n, Bh.p, Bl.p));
     CUtensorMap mAh, mAl, mBh, mBl;
     RL_TRY(make_tile_map(mAh, Ah.p, m, kp));
     RL_TRY(make_tile_map(mAl, Al.p, m, kp));
@@ -336,7 +357,7 @@ inline rl_status sgemm_tc(int m, int n, int k, float alpha, const float *A, long
     RL_TRY_CUDA(cudaGetSymbolAddress(reinterpret_cast<void **>(&err), g_sgemm_tc_err));
     const dim3 grid((n + tc::BN - 1) / tc::BN, (m + tc::BM - 1) / tc::BM);
     RL_LAUNCH(sgemm_tma_kernel, grid, tc::THREADS, tc::SMEM_BYTES, s, mAh, mAl, mBh, mBl, m, n, kp, alpha, beta, C,
-              ldc, err);
+              ldc, lower ? 1 : 0, err);
     return RL_OK;
 }
 

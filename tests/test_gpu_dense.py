@@ -59,12 +59,12 @@ def test_gemm_normwise(gpu, dtype, m, k, n):
     assert fro(got.astype(np.float64) - ref) <= max(k, 1) * eps * fro(a) * fro(b)
 
 
-@pytest.mark.parametrize("m,k,n", [(128, 64, 128), (256, 256, 256), (200, 100, 300), (130, 70, 131),
-                                   (1024, 512, 768), (2048, 2048, 2048)])
+@pytest.mark.parametrize("m,k,n", [(128, 256, 128), (256, 256, 256), (200, 300, 300), (130, 270, 131),
+                                   (64, 1000, 256), (1024, 512, 768), (2048, 2048, 2048)])
 def test_sgemm_tensor_core_elementwise(gpu, m, k, n):
-    """Shapes that take the tcgen05 3xTF32 path (at least one 128 x 128 tile, k >= 64;
-    ragged edges included): every element within the FP32 dot-product bound
-    2 k eps (|A| |B|)."""
+    """Shapes that take the tcgen05 3xTF32 path (a 128 x 128 tile's worth of C, k >= 256;
+    ragged edges and a half-height tile included): every element within the FP32
+    dot-product bound 2 k eps (|A| |B|)."""
     rng = np.random.default_rng(m + 3 * k + 7 * n)
     a = rng.standard_normal((m, k)).astype(np.float32)
     b = rng.standard_normal((k, n)).astype(np.float32)
