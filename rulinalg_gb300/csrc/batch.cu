@@ -265,10 +265,10 @@ rl_status plan_init(rl_batch_plan *p, size_t count, const int32_t *n, const uint
     RL_TRY(upload(p->d_aoff, p->a_off, s));
     RL_TRY(upload(p->d_boff, p->b_off, s));
     RL_TRY(upload(p->d_order, order, s));
-    // Host-path chunks: up to 16 contiguous ranges of about equal matrix bytes, each with
+    // Host-path chunks: up to 8 contiguous ranges of about equal matrix bytes, each with
     // its own largest-first order.
     {
-        const int want = (int)std::min<size_t>(16, std::max<size_t>(1, count));
+        const int want = (int)std::min<size_t>(8, std::max<size_t>(1, count));
         std::vector<int> corder;
         corder.reserve(count);
         size_t i = 0;
