@@ -184,10 +184,10 @@ static __global__ void __launch_bounds__(256) lu_panel_kernel(T *P, long long ld
         }
         if (g == 0 && tid == 0) ipiv[j] = k0 + wi;
         __syncthreads();
-        const T p = prow[j];
+        const T inv_p = T(1) / prow[j];  // multipliers by the reciprocal: one division per column
         for (int r = max(j + 1 - r0, 0) + tid; r < nr; r += blockDim.x) {
             T *row = R + r * LDR;
-            const T l = row[j] / p;
+            const T l = row[j] * inv_p;
             row[j] = l;
             for (int c = j + 1; c < kb; c++) row[c] = fma(-l, prow[c], row[c]);
         }
@@ -199,33 +199,85 @@ static __global__ void __launch_bounds__(256) lu_panel_kernel(T *P, long long ld
     }
 }
 
+// |v| as an unsigned key that orders like |v| (non-negative IEEE values order like
+// their bits), 0 for NaN, which never wins: the pivot search compares keys on the
+// integer pipe. On GB300 an FP64 comparison issues on the FP64 pipe, which a warp
+// occupies for tens of cycles; the integer form also keeps FP32 and FP64 alike.
+__device__ __forceinline__ unsigned long long amax_key(float v) {
+    const unsigned u = __float_as_uint(v) & 0x7fffffffu;
+    return u > 0x7f800000u ? 0ull : (unsigned long long)u + 1ull;
+}
+__device__ __forceinline__ unsigned long long amax_key(double v) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+    return u > 0x7ff0000000000000ull ? 0ull : u + 1ull;
+}
+
+// Largest key over the warp and the smallest index among the lanes holding it, in every
+// lane, on the redux instructions (keys of FP32 values fit in 32 bits; FP64 keys are
+// reduced high word first). Lanes without a candidate hold key 0 and index INT_MAX.
+template <class T>
+__device__ __forceinline__ void warp_amax_key(unsigned long long &k, int &i) {
+    bool top;
+    if (sizeof(T) == 4) {
+        const unsigned k32 = (unsigned)k;
+        const unsigned kmax = __reduce_max_sync(0xffffffffu, k32);
+        top = k32 == kmax;
+        k = kmax;
+    } else {
+        const unsigned hi = (unsigned)(k >> 32), lo = (unsigned)k;
+        const unsigned hmax = __reduce_max_sync(0xffffffffu, hi);
+        const unsigned lmax = __reduce_max_sync(0xffffffffu, hi == hmax ? lo : 0u);
+        top = hi == hmax && lo == lmax;
+        k = ((unsigned long long)hmax << 32) | lmax;
+    }
+    i = (int)__reduce_min_sync(0xffffffffu, top ? (unsigned)i : 0xffffffffu);
+}
+
 // LU panel on one thread-block cluster (up to 16 CTAs): the same algorithm as
-// lu_panel_kernel with the cross-CTA exchange moved on chip. CTA q owns rows
-// [q * rows_per, ...) in shared memory; per column every CTA publishes its candidate
-// (|v|, row, the row's values) and, if it holds it, row j in its own shared memory, one
-// cluster barrier makes them visible, and every CTA reads the candidates of all CTAs
-// through distributed shared memory and picks the same winner. Candidate slots are
-// double-buffered by column parity, so one barrier per column suffices. Every CTA runs
-// the same number of barriers (a failing pivot is seen by all at the same column) and
-// a last barrier keeps each CTA's shared memory alive until no other CTA reads it.
+// lu_panel_kernel with the cross-CTA exchange moved on chip. CTA g owns rows
+// [g * rows_per, ...) in shared memory; inside a CTA, `tpr` consecutive threads (1, 2, 4
+// or 8) share each row, thread q of a row owning the columns c = q (mod tpr), and thread
+// group t the rows t, t + 256 / tpr, ... The panel's row updates run at the SM's FP64
+// rate, so spreading a few rows over all four schedulers of every SM of the cluster is
+// what shortens a column. Per column:
+//   1. each thread searches column j of its rows (the thread that wrote them), the warps
+//      reduce on integer keys, one CTA barrier, every thread combines the warps' maxima;
+//   2. the CTA copies its candidate row (and row j, if it holds it) into a local slot and
+//      pushes its record (key, row, 1 / pivot) into slot g of every CTA's record table
+//      by remote shared-memory stores;
+//   3. one cluster barrier (release / acquire); every warp picks the same winner from its
+//      own CTA's table; threads c < kb read column c of the winning row and of row j
+//      from the CTAs that hold them (one remote round trip); one CTA barrier;
+//   4. the swap and the update run at once, each element stored by one thread: thread
+//      c < kb stores column c of the new row j and, for c < j, of row wi; the threads of
+//      row wi compute its columns >= j from the old row j; every other row below j
+//      updates itself, the multiplier broadcast within the row's threads by a shuffle.
+// Slots and records are double-buffered by column parity: a CTA writes slot s again only
+// after the next cluster barrier, which every CTA reaches after it has read slot s. Every
+// CTA runs the same barrier sequence (a failing pivot is seen by all at the same column).
 template <class T>
 static __global__ void __launch_bounds__(256) lu_panel_cluster_kernel(T *P, long long lda, int mrows, int kb, int k0,
-                                                              int rows_per, int *ipiv, int *err, T tiny) {
+                                                              int rows_per, int tpr, int *ipiv, int *err, T tiny) {
     namespace cg = cooperative_groups;
     constexpr int NB = PanelNB<T>::value;
     constexpr int LDR = NB + 1;
-    constexpr int CS = 2 + NB;  // candidate record: |v|, row, then the row's values
+    constexpr int CMAX = 16;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *R = reinterpret_cast<T *>(smem_raw);    // rows_per x LDR
-    T *cand = R + (size_t)rows_per * LDR;      // 2 x CS, this CTA's candidate per parity
-    T *rowj = cand + 2 * CS;                   // 2 x NB, row j when this CTA holds it
-    T *prow = rowj + 2 * NB;                   // NB, the pivot row
-    __shared__ T s_v[8];
-    __shared__ int s_i[8], s_q[8];
+    T *cand = R + (size_t)rows_per * LDR;      // 2 x NB, this CTA's candidate row per parity
+    T *rowj = cand + 2 * NB;                   // 2 x NB, row j when this CTA holds it
+    T *prow = rowj + 2 * NB;                   // NB, the pivot row (the new row j)
+    T *oldj = prow + NB;                       // NB, the old row j (the new row wi)
+    __shared__ unsigned long long s_k[8], rec_k[2 * CMAX];
+    __shared__ int s_i[8], rec_i[2 * CMAX];
+    __shared__ T rec_inv[2 * CMAX];
     cg::cluster_group cluster = cg::this_cluster();
     const int C = (int)cluster.num_blocks(), g = (int)cluster.block_rank();
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int r0 = g * rows_per, r1 = min(mrows, r0 + rows_per), nr = max(0, r1 - r0);
+    const int q = tid & (tpr - 1), grp = tid / tpr, G = (int)blockDim.x / tpr;
+    const int rpt = (rows_per + G - 1) / G;  // rows per thread group, the same in every thread
+    const unsigned long long ktiny = amax_key(tiny);
     if (g == 0)
         for (int j = tid; j < kb; j += blockDim.x) ipiv[j] = k0 + j;
     for (int idx = tid; idx < nr * kb; idx += blockDim.x) {
@@ -234,90 +286,95 @@ static __global__ void __launch_bounds__(256) lu_panel_cluster_kernel(T *P, long
     }
     __syncthreads();
     for (int j = 0; j < kb; j++) {
-        const int slot = j & 1;
-        // local candidate
-        T bv = T(-1);
+        const int slot = j & 1, qj = j & (tpr - 1);
+        // 1. local candidate
+        unsigned long long bk = 0ull;
         int bi = INT_MAX;
-        for (int r = max(j - r0, 0) + tid; r < nr; r += blockDim.x) {
-            const T v = absT(R[r * LDR + j]);
-            if (v > bv) {
-                bv = v;
-                bi = r0 + r;
-            }
-        }
-        warp_amax(bv, bi);
-        if (lane == 0) {
-            s_v[warp] = bv;
-            s_i[warp] = bi;
-        }
-        __syncthreads();
-        bv = s_v[0];
-        bi = s_i[0];
-        for (int w = 1; w < (int)(blockDim.x >> 5); w++) amax_combine(bv, bi, s_v[w], s_i[w]);
-        T *mine = cand + slot * CS;
-        if (tid == 0) {
-            mine[0] = bv;
-            mine[1] = (T)(bi == INT_MAX ? -1 : bi);
-        }
-        if (bi != INT_MAX && tid < kb) mine[2 + tid] = R[(bi - r0) * LDR + tid];
-        if (j >= r0 && j < r1 && tid < kb) rowj[slot * NB + tid] = R[(j - r0) * LDR + tid];
-        cluster.sync();
-        // the winner over the cluster, identical in every CTA (warp 0: lane q reads CTA q)
-        if (warp == 0) {
-            T wv = T(-1);
-            int wi = INT_MAX, wg = -1;
-            if (lane < C) {
-                const T *c = cluster.map_shared_rank(cand + slot * CS, lane);
-                const T v = c[0];
-                const int i = (int)c[1];
-                if (i >= 0) {
-                    wv = v;
-                    wi = i;
-                    wg = lane;
+        if (q == qj)
+            for (int k = 0; k < rpt; k++) {
+                const int r = grp + k * G;
+                if (r < nr && r0 + r >= j) {
+                    const unsigned long long key = amax_key(R[r * LDR + j]);
+                    if (key > bk) {
+                        bk = key;
+                        bi = r0 + r;
+                    }
                 }
             }
-            warp_amax3(wv, wi, wg);
-            if (lane == 0) {
-                s_v[0] = wv;
-                s_i[0] = wi;
-                s_q[0] = wg;
+        warp_amax_key<T>(bk, bi);
+        if (lane == 0) {
+            s_k[warp] = bk;
+            s_i[warp] = bi;
+        }
+        __syncthreads();  // also: every row's update for the previous column is done
+        bk = s_k[0];
+        bi = s_i[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
+            const unsigned long long k2 = s_k[w];
+            const int i2 = s_i[w];
+            if (k2 > bk || (k2 == bk && i2 < bi)) {
+                bk = k2;
+                bi = i2;
             }
         }
-        __syncthreads();
-        const T wv = s_v[0];
-        int wi = s_i[0], wg = s_q[0];
-        if (wi == INT_MAX) {  // no finite candidate (NaN column): keep the diagonal
+        // 2. local copies of the candidate row and row j; the record to every CTA
+        if (bk != 0ull && tid < kb) cand[slot * NB + tid] = R[(bi - r0) * LDR + tid];
+        if (j >= r0 && j < r1 && tid < kb) rowj[slot * NB + tid] = R[(j - r0) * LDR + tid];
+        if (warp == 0) {
+            const T inv = bk != 0ull ? T(1) / R[(bi - r0) * LDR + j] : T(0);
+            if (lane < C) {
+                const int e = slot * CMAX + g;
+                *cluster.map_shared_rank(rec_k + e, lane) = bk;
+                *cluster.map_shared_rank(rec_i + e, lane) = bk != 0ull ? bi : INT_MAX;
+                *cluster.map_shared_rank(rec_inv + e, lane) = inv;
+            }
+        }
+        cluster.sync();
+        // 3. the winner, the same in every warp of every CTA
+        unsigned long long wk = lane < C ? rec_k[slot * CMAX + lane] : 0ull;
+        int wi = lane < C ? rec_i[slot * CMAX + lane] : INT_MAX;
+        warp_amax_key<T>(wk, wi);
+        int wg = -1;
+        if (wk != 0ull) {
+            if (wk < ktiny) {  // the same decision in every CTA
+                if (g == 0 && tid == 0) atomicCAS(err, 0, RL_ERR_DIV_BY_ZERO);
+                break;
+            }
+            wg = wi / rows_per;
+        } else {  // no finite candidate (NaN column): keep the diagonal
             wi = j;
-            wg = -1;
         }
-        const bool stop = wg >= 0 && wv < tiny;  // the same decision in every CTA
-        const int owner_j = j / rows_per;        // the CTA holding row j
-        if (!stop && tid < kb) {
-            const T *src = wg >= 0 ? cluster.map_shared_rank(cand + slot * CS, wg) + 2
-                                   : cluster.map_shared_rank(rowj + slot * NB, owner_j);
-            prow[tid] = src[tid];
-        }
-        if (stop) {
-            if (g == 0 && tid == 0) atomicCAS(err, 0, RL_ERR_DIV_BY_ZERO);
-            break;
-        }
-        __syncthreads();
-        if (wi != j) {
-            if (j >= r0 && j < r1 && tid < kb) R[(j - r0) * LDR + tid] = prow[tid];
-            if (wi >= r0 && wi < r1 && tid < kb)
-                R[(wi - r0) * LDR + tid] = cluster.map_shared_rank(rowj + slot * NB, owner_j)[tid];
+        const int owner_j = j / rows_per;
+        if (tid < kb) {
+            const T o = cluster.map_shared_rank(rowj + slot * NB, owner_j)[tid];
+            oldj[tid] = o;
+            prow[tid] = wg >= 0 ? cluster.map_shared_rank(cand + slot * NB, wg)[tid] : o;
         }
         if (g == 0 && tid == 0) ipiv[j] = k0 + wi;
         __syncthreads();
-        const T p = prow[j];
-        for (int r = max(j + 1 - r0, 0) + tid; r < nr; r += blockDim.x) {
-            T *row = R + r * LDR;
-            const T l = row[j] / p;
-            row[j] = l;
-            for (int c = j + 1; c < kb; c++) row[c] = fma(-l, prow[c], row[c]);
+        const T inv_p = wg >= 0 ? rec_inv[slot * CMAX + wg] : T(1) / oldj[j];
+        // 4. swap and update
+        if (wi != j && tid < kb) {
+            if (j >= r0 && j < r1) R[(j - r0) * LDR + tid] = prow[tid];
+            if (wi >= r0 && wi < r1 && tid < j) R[(wi - r0) * LDR + tid] = oldj[tid];
         }
-        __syncthreads();
+        const int cfirst = j + 1 + ((q - j - 1) & (tpr - 1));  // this thread's first column > j
+        for (int k = 0; k < rpt; k++) {
+            const int r = grp + k * G, gr = r0 + r;
+            const bool valid = r < nr && gr > j;
+            T *row = R + (size_t)(valid ? r : 0) * LDR;
+            const T *src = gr == wi ? oldj : row;
+            T l = T(0);
+            if (valid && q == qj) l = src[j] * inv_p;
+            if (tpr > 1) l = __shfl_sync(0xffffffffu, l, qj, tpr);
+            if (valid) {
+                if (q == qj) row[j] = l;
+#pragma unroll 4
+                for (int c = cfirst; c < kb; c += tpr) row[c] = fma(-l, prow[c], src[c]);
+            }
+        }
     }
+    __syncthreads();
     for (int idx = tid; idx < nr * kb; idx += blockDim.x) {
         const int r = idx / kb, c = idx - r * kb;
         P[(long long)(r0 + r) * lda + c] = R[r * LDR + c];

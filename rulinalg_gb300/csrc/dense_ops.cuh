@@ -90,13 +90,14 @@ int probe_cluster(K kern, size_t smem) {
 }
 
 // Cluster size and rows per CTA for a panel of mrows rows of row_bytes each plus `extra`
-// bytes per CTA: the fewest CTAs with at most kClusterSmem bytes each (and at least
-// ceil(mrows / 256) CTAs), or 0 when that exceeds cmax.
-constexpr size_t kClusterSmem = 200 * 1024;
+// bytes per CTA: as many CTAs as keep at least 32 rows each (up to cmax; the panel's
+// update is bound by each SM's FP64 rate, so every SM added shortens a column), or 0
+// when even cmax CTAs would need more than kClusterSmem bytes each.
+constexpr size_t kClusterSmem = 224 * 1024;
 inline int cluster_shape(int mrows, size_t row_bytes, size_t extra, int cmax, int &rows_per) {
     const int cmin = (int)(((size_t)mrows * row_bytes + (kClusterSmem - extra) - 1) / (kClusterSmem - extra));
-    int C = std::max(cmin, ceil_div(mrows, 256));
-    if (C > cmax) return 0;
+    if (cmin > cmax || cmax == 0) return 0;
+    int C = std::max(cmin, std::min(cmax, ceil_div(mrows, 32)));
     C = std::max(C, 2);
     rows_per = ceil_div(mrows, C);
     return C;
@@ -129,12 +130,14 @@ rl_status lu_panel_cluster(T *P, long long lda, int mrows, int kb, int k0, int *
     launched = false;
     auto kern = lu_panel_cluster_kernel<T>;
     static const int cmax = probe_cluster(kern, kClusterSmem);
-    const size_t row_bytes = (NB + 1) * sizeof(T), extra = (2 * (2 + NB) + 3 * NB) * sizeof(T);
+    const size_t row_bytes = (NB + 1) * sizeof(T), extra = 6 * NB * sizeof(T);
     int rows_per = 0;
     const int C = cluster_shape(mrows, row_bytes, extra, cmax, rows_per);
     if (C == 0) return RL_OK;
-    RL_TRY(launch_cluster(kern, C, (size_t)rows_per * row_bytes + extra, s, P, lda, mrows, kb, k0, rows_per, ipiv, err,
-                          tiny));
+    int tpr = 1;  // threads per row: every thread busy when the CTA holds few rows
+    while (tpr < 8 && rows_per * tpr * 2 <= 256) tpr *= 2;
+    RL_TRY(launch_cluster(kern, C, (size_t)rows_per * row_bytes + extra, s, P, lda, mrows, kb, k0, rows_per, tpr, ipiv,
+                          err, tiny));
     launched = true;
     return RL_OK;
 }
