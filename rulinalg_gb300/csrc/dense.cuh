@@ -35,6 +35,10 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
+__device__ __forceinline__ int ld_acquire(const int *p) { return (int)ld_acquire_u32(reinterpret_cast<const unsigned *>(p)); }
+__device__ __forceinline__ void st_release(int *p, int v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 
 static __device__ bool grid_barrier(unsigned *ctr, unsigned target, int *err) {
     __shared__ int s_ok;
@@ -588,24 +592,94 @@ static __global__ void __launch_bounds__(256) qr_panel_cluster_kernel(T *P, long
 
 // ------------------------------------------------------------------- row swaps --
 // Applies ipiv[j0..j1) (global rows; step j swaps rows j and ipiv[j]) to the columns
-// [0, c_skip0) and [c_skip1, ncols) of A. Thread per column, swaps in order.
+// [0, c_skip0) and [c_skip1, ncols) of A, 64 columns per CTA, in blocks of 64 pivots:
+// the rows a block touches (its own 64 rows and the pivot rows outside them, at most
+// 128) are staged in shared memory with all loads in flight at once, the block's swaps
+// run there in order (thread per column), and the rows are written back. A swap chain
+// applied straight to global memory would wait one memory round trip per pivot.
+constexpr int kSwapCols = 64, kSwapBlock = 64;
 template <class T>
-static __global__ void laswp_kernel(T *A, long long lda, int ncols, int c_skip0, int c_skip1, const int *ipiv, int j0,
-                             int j1) {
+static __global__ void __launch_bounds__(256) laswp_kernel(T *A, long long lda, int ncols, int c_skip0, int c_skip1,
+                                                    const int *ipiv, int j0, int j1) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *S = reinterpret_cast<T *>(smem_raw);  // 2 * kSwapBlock slots x kSwapCols columns
+    __shared__ int s_piv[kSwapBlock], s_slot[kSwapBlock], s_row[2 * kSwapBlock];
+    const int tid = threadIdx.x, t = tid & (kSwapCols - 1), quarter = tid / kSwapCols;
     const int nother = ncols - (c_skip1 - c_skip0);
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= nother) return;
+    const int c = blockIdx.x * kSwapCols + t;
+    const bool act = c < nother;
     const int gc = c < c_skip0 ? c : c + (c_skip1 - c_skip0);
-    for (int j = j0; j < j1; j++) {
-        const int p = ipiv[j];
-        if (p != j) {
-            T *a = A + (long long)j * lda + gc;
-            T *b = A + (long long)p * lda + gc;
-            const T t = *a;
-            *a = *b;
-            *b = t;
+    for (int b = j0; b < j1; b += kSwapBlock) {
+        const int kb = min(kSwapBlock, j1 - b);
+        if (tid < kb) s_piv[tid] = ipiv[b + tid];
+        __syncthreads();
+        // slot of each pivot row: its place in [b, b + kb), else an outside slot named
+        // by the first step that swaps it in (the slot that stages it)
+        if (tid < kb) {
+            const int p = s_piv[tid];
+            int sl;
+            if (p >= b && p < b + kb) {
+                sl = p - b;
+            } else {
+                int first = tid;
+                for (int u = 0; u < tid; u++)
+                    if (s_piv[u] == p) {
+                        first = u;
+                        break;
+                    }
+                sl = kSwapBlock + first;
+            }
+            s_slot[tid] = sl;
+            s_row[tid] = b + tid;
+            s_row[kSwapBlock + tid] = sl == kSwapBlock + tid ? p : -1;
+        } else if (tid < kSwapBlock) {
+            s_row[tid] = -1;
+            s_row[kSwapBlock + tid] = -1;
         }
+        __syncthreads();
+        if (act) {
+            T v[2 * kSwapBlock / 4];
+#pragma unroll
+            for (int i = 0; i < 2 * kSwapBlock / 4; i++) {
+                const int r = s_row[quarter + 4 * i];
+                v[i] = r >= 0 ? A[(long long)r * lda + gc] : T(0);
+            }
+#pragma unroll
+            for (int i = 0; i < 2 * kSwapBlock / 4; i++) S[(quarter + 4 * i) * kSwapCols + t] = v[i];
+        }
+        __syncthreads();
+        if (act && quarter == 0)
+            for (int u = 0; u < kb; u++) {
+                const int sl = s_slot[u];
+                if (sl != u) {
+                    const T x = S[u * kSwapCols + t];
+                    S[u * kSwapCols + t] = S[sl * kSwapCols + t];
+                    S[sl * kSwapCols + t] = x;
+                }
+            }
+        __syncthreads();
+        if (act)
+#pragma unroll 4
+            for (int i = 0; i < 2 * kSwapBlock / 4; i++) {
+                const int sl = quarter + 4 * i, r = s_row[sl];
+                if (r >= 0) A[(long long)r * lda + gc] = S[sl * kSwapCols + t];
+            }
+        __syncthreads();  // the staging area and slot map are reused by the next block
     }
+}
+
+// Launch of laswp_kernel over the columns outside [c_skip0, c_skip1).
+template <class T>
+rl_status laswp(T *A, long long lda, int ncols, int c_skip0, int c_skip1, const int *ipiv, int j0, int j1,
+                cudaStream_t s) {
+    const int nother = ncols - (c_skip1 - c_skip0);
+    if (nother <= 0 || j1 <= j0) return RL_OK;
+    const size_t smem = sizeof(T) * 2 * kSwapBlock * kSwapCols;
+    static const cudaError_t attr =
+        cudaFuncSetAttribute(laswp_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    RL_TRY_CUDA(attr);
+    RL_LAUNCH(laswp_kernel<T>, ceil_div(nother, kSwapCols), 256, smem, s, A, lda, ncols, c_skip0, c_skip1, ipiv, j0, j1);
+    return RL_OK;
 }
 
 // ------------------------------------------------------- diagonal-block solves --
@@ -656,6 +730,167 @@ static __global__ void __launch_bounds__(64) trsm_diag_kernel(const T *D, long l
         return;
     }
     for (int i = 0; i < bs; i++) Y[(long long)i * ldy + c] = Ys[i][t];
+}
+
+// ------------------------------------------- few-right-hand-side triangular sweep --
+// op(A) X = Y in place for nrhs <= 8 right-hand sides in ONE launch: CTA per 64-row
+// block of the solution, blocks taken in solve order by an atomic ticket (forward for
+// modes 0 / 1, backward for modes 2 / 3; the modes are those of tri_solve_dev). A block
+// folds in the contribution of every block solved before it as each one is published
+// (its flag in `ready`), overlapping that GEMV work with the blocks still being solved,
+// then solves its diagonal block by substitution (one warp per right-hand side, the
+// multipliers by the diagonal's reciprocals) and publishes its rows. A CTA waits only on
+// tickets taken before its own, by CTAs that are already running, so the sweep always
+// progresses; every wait is also bounded by kBarrierTimeoutNs (RL_ERR_TIMEOUT).
+// Per-launch state: ctl[0] = ticket, ctl[1 + b] = block b published, zeroed by the host.
+constexpr int kSweepRows = 64, kSweepRhs = 8;
+template <class T>
+static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const T *__restrict__ A, long long lda, int n,
+                                                             T *__restrict__ Y, long long ldy, int nrhs, int mode,
+                                                             int *ctl, int *status, T tiny) {
+    constexpr int BR = kSweepRows, LDD = BR + 1;
+    __shared__ T Ds[BR * LDD];           // the diagonal block
+    __shared__ T inv[BR];                 // 1 / d_ii
+    __shared__ T xs[BR * kSweepRhs];      // a published block's solution, then the folded sums
+    __shared__ int s_b, s_fail;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nb = (n + BR - 1) / BR;
+    const bool fwd = mode <= 1, trans = mode == 3;
+    if (tid == 0) {
+        const int t = atomicAdd(ctl, 1);
+        s_b = fwd ? t : nb - 1 - t;
+        s_fail = 0;
+    }
+    __syncthreads();
+    const int b = s_b, r0 = b * BR, bs = min(BR, n - r0);
+    // the diagonal block and its reciprocal diagonal: no dependence on other blocks
+    for (int idx = tid; idx < bs * bs; idx += blockDim.x) {
+        const int i = idx / bs, j = idx - i * bs;
+        Ds[i * LDD + j] = A[(long long)(r0 + i) * lda + r0 + j];
+    }
+    __syncthreads();
+    if (tid < bs) {
+        const T d = Ds[tid * LDD + tid];
+        if (mode != 0 && absT(d) < tiny) atomicCAS(status, 0, RL_ERR_DIV_BY_ZERO);
+        inv[tid] = mode == 0 ? T(1) : T(1) / d;
+    }
+    // thread (row r, quarter q): non-transposed reads A[r][q * 16 + jj] (a thread's 16
+    // columns contiguous), transposed reads A[q * 16 + jj][r] (a warp's rows contiguous)
+    const int r = trans ? (tid & (BR - 1)) : (tid >> 2), q = trans ? (tid >> 6) : (tid & 3);
+    T acc[kSweepRhs];
+#pragma unroll
+    for (int c = 0; c < kSweepRhs; c++) acc[c] = T(0);
+    const int nk = fwd ? b : nb - 1 - b;  // blocks solved before this one
+    for (int kk = 0; kk < nk; kk++) {
+        const int k = fwd ? kk : nb - 1 - kk, c0 = k * BR, ks = min(BR, n - c0);
+        T a[16];
+#pragma unroll
+        for (int jj = 0; jj < 16; jj++) {
+            const int j = q * 16 + jj;
+            a[jj] = (r < bs && j < ks)
+                        ? (trans ? A[(long long)(c0 + j) * lda + r0 + r] : A[(long long)(r0 + r) * lda + c0 + j])
+                        : T(0);
+        }
+        if (tid == 0) {
+            const unsigned long long t0 = global_ns();
+            while (ld_acquire(ctl + 1 + k) == 0) {
+                if (global_ns() - t0 > kBarrierTimeoutNs) {
+                    s_fail = 1;
+                    break;
+                }
+            }
+        }
+        __syncthreads();
+        if (s_fail) break;
+        for (int idx = tid; idx < ks * nrhs; idx += blockDim.x) {
+            const int i = idx / nrhs, c = idx - i * nrhs;
+            xs[i * kSweepRhs + c] = __ldcg(Y + (long long)(c0 + i) * ldy + c);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int jj = 0; jj < 16; jj++) {
+            const int j = q * 16 + jj;
+#pragma unroll
+            for (int c = 0; c < kSweepRhs; c++)
+                if (c < nrhs) acc[c] = fma(a[jj], xs[j * kSweepRhs + c], acc[c]);
+        }
+        __syncthreads();  // xs is refilled for the next block
+    }
+    // sum of the 4 column quarters of each row into xs
+    if (!trans) {
+#pragma unroll
+        for (int c = 0; c < kSweepRhs; c++) {
+            acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 1);
+            acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 2);
+        }
+        if (q == 0)
+#pragma unroll
+            for (int c = 0; c < kSweepRhs; c++) xs[r * kSweepRhs + c] = acc[c];
+        __syncthreads();
+    } else {
+        for (int qq = 0; qq < 4; qq++) {
+            if (q == qq)
+#pragma unroll
+                for (int c = 0; c < kSweepRhs; c++) xs[r * kSweepRhs + c] = (qq ? xs[r * kSweepRhs + c] : T(0)) + acc[c];
+            __syncthreads();
+        }
+    }
+    // substitution: warp c solves right-hand side c; lane l holds rows l and l + 32
+    if (warp < nrhs && !s_fail) {
+        const int c = warp;
+        T y[2];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int i = lane + 32 * h;
+            T v = T(0);
+            if (i < bs) v = __ldcg(Y + (long long)(r0 + i) * ldy + c) - xs[i * kSweepRhs + c];
+            y[h] = v;
+        }
+        if (fwd) {
+            for (int k = 0; k < bs; k++) {
+                const int h = k >> 5;
+                T xk = __shfl_sync(0xffffffffu, h ? y[1] : y[0], k & 31) * inv[k];
+                if (lane == (k & 31)) {
+                    if (h)
+                        y[1] = xk;
+                    else
+                        y[0] = xk;
+                }
+#pragma unroll
+                for (int hh = 0; hh < 2; hh++) {
+                    const int i = lane + 32 * hh;
+                    if (i > k && i < bs) y[hh] = fma(-Ds[i * LDD + k], xk, y[hh]);
+                }
+            }
+        } else {
+            for (int k = bs - 1; k >= 0; k--) {
+                const int h = k >> 5;
+                T xk = __shfl_sync(0xffffffffu, h ? y[1] : y[0], k & 31) * inv[k];
+                if (lane == (k & 31)) {
+                    if (h)
+                        y[1] = xk;
+                    else
+                        y[0] = xk;
+                }
+#pragma unroll
+                for (int hh = 0; hh < 2; hh++) {
+                    const int i = lane + 32 * hh;
+                    if (i < k) y[hh] = fma(-(trans ? Ds[k * LDD + i] : Ds[i * LDD + k]), xk, y[hh]);
+                }
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int i = lane + 32 * h;
+            if (i < bs) __stcg(Y + (long long)(r0 + i) * ldy + c, y[h]);
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        if (s_fail) atomicCAS(status, 0, RL_ERR_TIMEOUT);
+        __threadfence();
+        st_release(ctl + 1 + b, 1);  // published even after a timeout, so no later block waits forever
+    }
 }
 
 // Row-wise solve X D^T = Y for the rows of Y (m x bs, stride ldy), D lower bs x bs:

@@ -197,7 +197,7 @@ rl_status lu_factor_dev(T *A, long long lda, int n, int *ipiv, cudaStream_t s, T
         }
         const int nother = n - kb;
         if (nother > 0)
-            RL_LAUNCH(laswp_kernel<T>, ceil_div(nother, 256), 256, 0, s, A, lda, n, k0, k0 + kb, ipiv, k0, k0 + kb);
+            RL_TRY(laswp<T>(A, lda, n, k0, k0 + kb, ipiv, k0, k0 + kb, s));
         const int n2 = n - k0 - kb;
         if (n2 > 0) {
             DevBuf<int> st;
@@ -329,37 +329,14 @@ rl_status tri_solve_dev(const T *A, long long lda, int n, T *Y, long long ldy, i
                         cudaStream_t s, T tiny = Eps<T>::value) {
     if (n <= 0 || nrhs <= 0) return RL_OK;
     constexpr int NB = 64;
-    if (nrhs <= 8) {
-        // Few right-hand sides: warp-per-column diagonal blocks and warp-per-row GEMV
-        // updates (a GEMM tile would waste all but nrhs of its columns).
-        const int wpb = 8, gridr = std::max(1, std::min(4 * num_sms(), ceil_div(n, wpb)));
-        if (mode == 0 || mode == 1) {
-            for (int b0 = 0; b0 < n; b0 += NB) {
-                const int bs = std::min(NB, n - b0), rest = n - b0 - bs;
-                T *Yb = Y + (long long)b0 * ldy;
-                RL_LAUNCH(trsv_diag_kernel<T>, 1, 256, 0, s, A + (long long)b0 * lda + b0, lda, bs, Yb, ldy, nrhs, mode,
-                          dstatus, tiny);
-                if (rest > 0)
-                    RL_LAUNCH(gemv_update_kernel<T>, std::min(gridr, ceil_div(rest, wpb)), 32 * wpb, 0, s,
-                              A + (long long)(b0 + bs) * lda + b0, lda, rest, bs, Yb, ldy, Yb + (long long)bs * ldy,
-                              nrhs, false);
-            }
-        } else {
-            for (int b1 = n; b1 > 0; b1 -= NB) {
-                const int b0 = std::max(0, b1 - NB), bs = b1 - b0;
-                T *Yb = Y + (long long)b0 * ldy;
-                RL_LAUNCH(trsv_diag_kernel<T>, 1, 256, 0, s, A + (long long)b0 * lda + b0, lda, bs, Yb, ldy, nrhs, mode,
-                          dstatus, tiny);
-                if (b0 > 0) {
-                    if (mode == 2)
-                        RL_LAUNCH(gemv_update_kernel<T>, std::min(gridr, ceil_div(b0, wpb)), 32 * wpb, 0, s, A + b0, lda,
-                                  b0, bs, Yb, ldy, Y, nrhs, false);
-                    else
-                        RL_LAUNCH(gemv_update_kernel<T>, ceil_div(b0, 256), 256, 0, s, A + (long long)b0 * lda, lda, b0,
-                                  bs, Yb, ldy, Y, nrhs, true);
-                }
-            }
-        }
+    if (nrhs <= kSweepRhs) {
+        // Few right-hand sides: the whole solve in one launch (trsv_sweep_kernel); a GEMM
+        // tile per block would waste all but nrhs of its columns.
+        const int nb = ceil_div(n, kSweepRows);
+        DevBuf<int> ctl;
+        RL_TRY(ctl.alloc(1 + nb, s));
+        RL_TRY_CUDA(cudaMemsetAsync(ctl.p, 0, sizeof(int) * (1 + nb), s));
+        RL_LAUNCH(trsv_sweep_kernel<T>, nb, 256, 0, s, A, lda, n, Y, ldy, nrhs, mode, ctl.p, dstatus, tiny);
         return RL_OK;
     }
     const size_t tsm = sizeof(T) * (64 * 65 + 64 * 64);

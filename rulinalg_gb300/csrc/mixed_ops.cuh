@@ -56,7 +56,7 @@ inline rl_status precond_solve(const float *F, int n, int kind, const int *ipiv,
                         int *dstatus, cudaStream_t s) {
     const float tiny = FLT_MIN;
     if (kind == RL_KIND_LU) {
-        RL_LAUNCH(laswp_kernel<float>, ceil_div(nrhs, 256), 256, 0, s, W, ldw, nrhs, 0, 0, ipiv, 0, n);
+        RL_TRY(laswp<float>(W, ldw, nrhs, 0, 0, ipiv, 0, n, s));
         RL_TRY(tri_solve_dev<float>(F, n, n, W, ldw, nrhs, 0, dstatus, s, tiny));
         return tri_solve_dev<float>(F, n, n, W, ldw, nrhs, 2, dstatus, s, tiny);
     }
@@ -195,7 +195,7 @@ inline rl_status solve_fp64(const double *A, long long lda, int n, int kind, con
                                   cudaMemcpyDeviceToDevice, s));
     if (kind == RL_KIND_LU) {
         RL_TRY(lu_factor_dev<double>(F.p, n, n, ipiv.p, s));
-        RL_LAUNCH(laswp_kernel<double>, ceil_div(nrhs, 256), 256, 0, s, X, ldx, nrhs, 0, 0, ipiv.p, 0, n);
+        RL_TRY(laswp<double>(X, ldx, nrhs, 0, 0, ipiv.p, 0, n, s));
         RL_TRY(tri_solve_dev<double>(F.p, n, n, X, ldx, nrhs, 0, st.p, s));
         RL_TRY(tri_solve_dev<double>(F.p, n, n, X, ldx, nrhs, 2, st.p, s));
     } else {
@@ -336,7 +336,7 @@ struct MixedFactor {
         RL_TRY_CUDA(cudaMemcpy2DAsync(X, ldx * sizeof(double), B, ldb * sizeof(double), nrhs * sizeof(double), n,
                                       cudaMemcpyDeviceToDevice, s));
         if (kind == RL_KIND_LU) {
-            RL_LAUNCH(laswp_kernel<double>, ceil_div(nrhs, 256), 256, 0, s, X, ldx, nrhs, 0, 0, ipiv64, 0, n);
+            RL_TRY(laswp<double>(X, ldx, nrhs, 0, 0, ipiv64, 0, n, s));
             RL_TRY(tri_solve_dev<double>(F64, n, n, X, ldx, nrhs, 0, st.p, s));
             RL_TRY(tri_solve_dev<double>(F64, n, n, X, ldx, nrhs, 2, st.p, s));
         } else {
