@@ -685,51 +685,76 @@ rl_status laswp(T *A, long long lda, int ncols, int c_skip0, int c_skip1, const 
 // ------------------------------------------------------- diagonal-block solves --
 // Solves op(D) X = Y in place for the bs x bs diagonal block D (bs <= 64, row stride
 // ldd) and Y = bs x nrhs (row stride ldy). mode 0: D unit lower; 1: D lower; 2: D upper;
-// 3: D^T with D lower (L^T). One thread per right-hand-side column. |d_ii| < tiny
-// (modes 1-3) records RL_ERR_DIV_BY_ZERO in status.
+// 3: D^T with D lower (L^T). |d_ii| < tiny (modes 1-3) records RL_ERR_DIV_BY_ZERO in
+// status and leaves Y unchanged. CTA per 8 columns, warp per 2 columns, 16 lanes per
+// column each holding 4 of its rows in registers: step j broadcasts x_j within the
+// column's lanes by a shuffle and every lane updates its rows, y_i -= d_ij x_j in
+// increasing j (the order of the reference's substitution). The FP64 work of a U12
+// solve is spread over every scheduler of every SM instead of a few CTAs' threads.
+constexpr int kTrsmCols = 8;
 template <class T>
-static __global__ void __launch_bounds__(64) trsm_diag_kernel(const T *D, long long ldd, int bs, T *Y, long long ldy,
-                                                       int nrhs, int mode, int *status, T tiny) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T (*Ds)[65] = reinterpret_cast<T (*)[65]>(smem_raw);             // 64 x 65
-    T (*Ys)[64] = reinterpret_cast<T (*)[64]>(smem_raw + sizeof(T) * 64 * 65);  // 64 x 64
-    const int t = threadIdx.x;
-    const int c = blockIdx.x * 64 + t;
-    for (int idx = t; idx < bs * bs; idx += 64) {
+static __global__ void __launch_bounds__(128) trsm_diag_kernel(const T *D, long long ldd, int bs, T *Y, long long ldy,
+                                                        int nrhs, int mode, int *status, T tiny) {
+    __shared__ T Ds[64][65];
+    __shared__ T Ys[64][kTrsmCols];
+    __shared__ int s_bad;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int c0 = blockIdx.x * kTrsmCols;
+    if (tid == 0) s_bad = 0;
+    for (int idx = tid; idx < bs * bs; idx += blockDim.x) {
         const int i = idx / bs, j = idx - i * bs;
         Ds[i][j] = D[(long long)i * ldd + j];
     }
-    if (c < nrhs)
-        for (int i = 0; i < bs; i++) Ys[i][t] = Y[(long long)i * ldy + c];
-    __syncthreads();
-    if (c >= nrhs) return;
-    int bad = 0;
-    if (mode == 0 || mode == 1) {
-        for (int i = 0; i < bs; i++) {
-            T s = Ys[i][t];
-            for (int j = 0; j < i; j++) s = fma(-Ds[i][j], Ys[j][t], s);
-            if (mode == 1) {
-                if (absT(Ds[i][i]) < tiny) bad = 1;
-                s = s / Ds[i][i];
-            }
-            Ys[i][t] = s;
-        }
-    } else {
-        for (int i = bs - 1; i >= 0; i--) {
-            T s = Ys[i][t];
-            if (mode == 2)
-                for (int j = i + 1; j < bs; j++) s = fma(-Ds[i][j], Ys[j][t], s);
-            else
-                for (int j = i + 1; j < bs; j++) s = fma(-Ds[j][i], Ys[j][t], s);
-            if (absT(Ds[i][i]) < tiny) bad = 1;
-            Ys[i][t] = s / Ds[i][i];
-        }
+    for (int idx = tid; idx < 64 * kTrsmCols; idx += blockDim.x) {
+        const int i = idx / kTrsmCols, cc = idx - i * kTrsmCols;
+        Ys[i][cc] = (i < bs && c0 + cc < nrhs) ? Y[(long long)i * ldy + c0 + cc] : T(0);
     }
-    if (bad) {
-        atomicCAS(status, 0, RL_ERR_DIV_BY_ZERO);
+    __syncthreads();
+    if (mode != 0 && tid < bs && absT(Ds[tid][tid]) < tiny) s_bad = 1;
+    __syncthreads();
+    if (s_bad) {
+        if (tid == 0) atomicCAS(status, 0, RL_ERR_DIV_BY_ZERO);
         return;
     }
-    for (int i = 0; i < bs; i++) Y[(long long)i * ldy + c] = Ys[i][t];
+    const int col = 2 * warp + (lane >> 4), r16 = lane & 15;
+    T y[4];
+#pragma unroll
+    for (int sl = 0; sl < 4; sl++) y[sl] = Ys[16 * sl + r16][col];
+    if (mode <= 1) {
+#pragma unroll
+        for (int j = 0; j < 64; j++) {
+            if (j < bs) {
+                if (mode == 1 && r16 == (j & 15)) y[j >> 4] = y[j >> 4] / Ds[j][j];
+                const T xj = __shfl_sync(0xffffffffu, y[j >> 4], j & 15, 16);
+#pragma unroll
+                for (int sl = j >> 4; sl < 4; sl++) {
+                    const int i = 16 * sl + r16;
+                    if (i > j && i < bs) y[sl] = fma(-Ds[i][j], xj, y[sl]);
+                }
+            }
+        }
+    } else {
+#pragma unroll
+        for (int j = 63; j >= 0; j--) {
+            if (j < bs) {
+                if (r16 == (j & 15)) y[j >> 4] = y[j >> 4] / Ds[j][j];
+                const T xj = __shfl_sync(0xffffffffu, y[j >> 4], j & 15, 16);
+#pragma unroll
+                for (int sl = 0; sl <= (j >> 4); sl++) {
+                    const int i = 16 * sl + r16;
+                    if (i < j) y[sl] = fma(-(mode == 2 ? Ds[i][j] : Ds[j][i]), xj, y[sl]);
+                }
+            }
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int sl = 0; sl < 4; sl++) Ys[16 * sl + r16][col] = y[sl];
+    __syncthreads();
+    for (int idx = tid; idx < bs * kTrsmCols; idx += blockDim.x) {
+        const int i = idx / kTrsmCols, cc = idx - i * kTrsmCols;
+        if (c0 + cc < nrhs) Y[(long long)i * ldy + c0 + cc] = Ys[i][cc];
+    }
 }
 
 // ------------------------------------------- few-right-hand-side triangular sweep --

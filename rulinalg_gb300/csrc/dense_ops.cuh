@@ -175,8 +175,6 @@ rl_status lu_factor_dev(T *A, long long lda, int n, int *ipiv, cudaStream_t s, T
     RL_TRY(sync.alloc(1, s));
     auto pk = lu_panel_kernel<T>;
     RL_TRY(set_smem(pk, 200 * 1024));
-    const size_t tsm = sizeof(T) * (64 * 65 + 64 * 64);
-    RL_TRY(set_smem(trsm_diag_kernel<T>, tsm));
     // The error word is sticky across panels (only the barrier counter is reset per
     // launch) and read once at the end: a failed panel leaves identity pivots, the work
     // after it runs on in-range indices, and every later panel stops at its first barrier.
@@ -203,7 +201,7 @@ rl_status lu_factor_dev(T *A, long long lda, int n, int *ipiv, cudaStream_t s, T
             DevBuf<int> st;
             RL_TRY(st.alloc(1, s));
             RL_TRY_CUDA(cudaMemsetAsync(st.p, 0, sizeof(int), s));
-            RL_LAUNCH(trsm_diag_kernel<T>, ceil_div(n2, 64), 64, tsm, s, P, lda, kb, P + kb, lda, n2, 0, st.p, tiny);
+            RL_LAUNCH(trsm_diag_kernel<T>, ceil_div(n2, kTrsmCols), 128, 0, s, P, lda, kb, P + kb, lda, n2, 0, st.p, tiny);
             RL_TRY((gemm<T, false, false>(n2, n2, kb, T(-1), P + (long long)kb * lda, lda, P + kb, lda, T(1),
                                          P + (long long)kb * lda + kb, lda, s)));
         }
@@ -339,15 +337,13 @@ rl_status tri_solve_dev(const T *A, long long lda, int n, T *Y, long long ldy, i
         RL_LAUNCH(trsv_sweep_kernel<T>, nb, 256, 0, s, A, lda, n, Y, ldy, nrhs, mode, ctl.p, dstatus, tiny);
         return RL_OK;
     }
-    const size_t tsm = sizeof(T) * (64 * 65 + 64 * 64);
-    RL_TRY(set_smem(trsm_diag_kernel<T>, tsm));
-    const int gr = ceil_div(nrhs, 64);
+    const int gr = ceil_div(nrhs, kTrsmCols);
     if (mode == 0 || mode == 1) {
         for (int b0 = 0; b0 < n; b0 += NB) {
             const int bs = std::min(NB, n - b0);
             const T *D = A + (long long)b0 * lda + b0;
             T *Yb = Y + (long long)b0 * ldy;
-            RL_LAUNCH(trsm_diag_kernel<T>, gr, 64, tsm, s, D, lda, bs, Yb, ldy, nrhs, mode, dstatus, tiny);
+            RL_LAUNCH(trsm_diag_kernel<T>, gr, 128, 0, s, D, lda, bs, Yb, ldy, nrhs, mode, dstatus, tiny);
             const int rest = n - b0 - bs;
             if (rest > 0)
                 RL_TRY((gemm<T, false, false>(rest, nrhs, bs, T(-1), A + (long long)(b0 + bs) * lda + b0, lda, Yb, ldy,
@@ -358,7 +354,7 @@ rl_status tri_solve_dev(const T *A, long long lda, int n, T *Y, long long ldy, i
             const int b0 = std::max(0, b1 - NB), bs = b1 - b0;
             const T *D = A + (long long)b0 * lda + b0;
             T *Yb = Y + (long long)b0 * ldy;
-            RL_LAUNCH(trsm_diag_kernel<T>, gr, 64, tsm, s, D, lda, bs, Yb, ldy, nrhs, mode, dstatus, tiny);
+            RL_LAUNCH(trsm_diag_kernel<T>, gr, 128, 0, s, D, lda, bs, Yb, ldy, nrhs, mode, dstatus, tiny);
             if (b0 > 0) {
                 if (mode == 2)
                     RL_TRY((gemm<T, false, false>(b0, nrhs, bs, T(-1), A + b0, lda, Yb, ldy, T(1), Y, ldy, s)));
