@@ -107,4 +107,11 @@ inline int ceil_div(long long a, long long b) { return static_cast<int>((a + b -
 
 int num_sms();
 
+// Set on threads that share the GPU with other streams of this library (the serving
+// loop's workers): kernels whose CTAs wait on other CTAs of the same launch, holding
+// their SMs meanwhile, are replaced there by chains of short launches. Measured on the
+// served stream: the one-launch triangular sweep next to the other workers' panels and
+// batched launches cut throughput from ~870 to ~390 requests/s.
+extern thread_local bool g_shared_gpu;
+
 }  // namespace rl

@@ -16,18 +16,14 @@ namespace {
 
 // ------------------------------------------------------------- host entry points --
 
-// The public GEMM: FP32 with at least one 128 x 128 tile (and K >= 64) runs on the
-// tensor cores (3xTF32, FP32 accuracy); everything else, and all FP64, on the SIMT kernel.
+// The public GEMM: FP32 with at least one 128 x 128 tile's worth of C and K >= 256 runs
+// on the tensor cores (3xTF32, FP32 accuracy); everything else, and all FP64, on the
+// SIMT kernel; both split a long K when the product has few output tiles (gemm()).
 template <class T>
 rl_status gemm_public(int m, int n, int k, const T *a, long long lda, const T *b, long long ldb, T *c, long long ldc,
                       cudaStream_t s, bool &used_tc) {
     used_tc = false;
-    if constexpr (std::is_same<T, float>::value) {
-        if (sgemm_tc_eligible(m, n, k)) {
-            used_tc = true;
-            return sgemm_tc<false, false>(m, n, k, 1.f, a, lda, b, ldb, 0.f, c, ldc, false, s);
-        }
-    }
+    if constexpr (std::is_same<T, float>::value) used_tc = sgemm_tc_eligible(m, n, k);
     return gemm<T, false, false>(m, n, k, T(1), a, lda, b, ldb, T(0), c, ldc, s);
 }
 

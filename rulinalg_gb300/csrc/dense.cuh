@@ -758,17 +758,19 @@ static __global__ void __launch_bounds__(128) trsm_diag_kernel(const T *D, long 
 }
 
 // ------------------------------------------- few-right-hand-side triangular sweep --
-// op(A) X = Y in place for nrhs <= 8 right-hand sides in ONE launch: CTA per 64-row
-// block of the solution, blocks taken in solve order by an atomic ticket (forward for
-// modes 0 / 1, backward for modes 2 / 3; the modes are those of tri_solve_dev). A block
-// folds in the contribution of every block solved before it as each one is published
-// (its flag in `ready`), overlapping that GEMV work with the blocks still being solved,
-// then solves its diagonal block by substitution (one warp per right-hand side, the
-// multipliers by the diagonal's reciprocals) and publishes its rows. A CTA waits only on
-// tickets taken before its own, by CTAs that are already running, so the sweep always
-// progresses; every wait is also bounded by kBarrierTimeoutNs (RL_ERR_TIMEOUT).
+// op(A) X = Y in place for nrhs <= 8 right-hand sides in ONE launch of at most
+// kSweepCtas CTAs: each CTA takes 64-row blocks of the solution in solve order by an
+// atomic ticket (forward for modes 0 / 1, backward for modes 2 / 3; the modes are those
+// of tri_solve_dev), one after another. A block folds in the contribution of every block
+// solved before it as each one is published (its flag in ctl), overlapping that GEMV
+// work with the blocks still being solved, then solves its diagonal block by
+// substitution (one warp per right-hand side, the multipliers by the diagonal's
+// reciprocals) and publishes its rows. A CTA waits only on tickets taken before its own,
+// by CTAs that are running, so the sweep always progresses; a waiting thread sleeps
+// between polls (other streams' kernels share the SMs), and every wait is bounded by
+// kBarrierTimeoutNs (RL_ERR_TIMEOUT).
 // Per-launch state: ctl[0] = ticket, ctl[1 + b] = block b published, zeroed by the host.
-constexpr int kSweepRows = 64, kSweepRhs = 8;
+constexpr int kSweepRows = 64, kSweepRhs = 8, kSweepCtas = 32;
 template <class T>
 static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const T *__restrict__ A, long long lda, int n,
                                                              T *__restrict__ Y, long long ldy, int nrhs, int mode,
@@ -777,144 +779,146 @@ static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const T *__restr
     __shared__ T Ds[BR * LDD];           // the diagonal block
     __shared__ T inv[BR];                 // 1 / d_ii
     __shared__ T xs[BR * kSweepRhs];      // a published block's solution, then the folded sums
-    __shared__ int s_b, s_fail;
+    __shared__ int s_t, s_fail;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nb = (n + BR - 1) / BR;
     const bool fwd = mode <= 1, trans = mode == 3;
-    if (tid == 0) {
-        const int t = atomicAdd(ctl, 1);
-        s_b = fwd ? t : nb - 1 - t;
-        s_fail = 0;
-    }
-    __syncthreads();
-    const int b = s_b, r0 = b * BR, bs = min(BR, n - r0);
-    // the diagonal block and its reciprocal diagonal: no dependence on other blocks
-    for (int idx = tid; idx < bs * bs; idx += blockDim.x) {
-        const int i = idx / bs, j = idx - i * bs;
-        Ds[i * LDD + j] = A[(long long)(r0 + i) * lda + r0 + j];
-    }
-    __syncthreads();
-    if (tid < bs) {
-        const T d = Ds[tid * LDD + tid];
-        if (mode != 0 && absT(d) < tiny) atomicCAS(status, 0, RL_ERR_DIV_BY_ZERO);
-        inv[tid] = mode == 0 ? T(1) : T(1) / d;
-    }
-    // thread (row r, quarter q): non-transposed reads A[r][q * 16 + jj] (a thread's 16
-    // columns contiguous), transposed reads A[q * 16 + jj][r] (a warp's rows contiguous)
-    const int r = trans ? (tid & (BR - 1)) : (tid >> 2), q = trans ? (tid >> 6) : (tid & 3);
-    T acc[kSweepRhs];
-#pragma unroll
-    for (int c = 0; c < kSweepRhs; c++) acc[c] = T(0);
-    const int nk = fwd ? b : nb - 1 - b;  // blocks solved before this one
-    for (int kk = 0; kk < nk; kk++) {
-        const int k = fwd ? kk : nb - 1 - kk, c0 = k * BR, ks = min(BR, n - c0);
-        T a[16];
-#pragma unroll
-        for (int jj = 0; jj < 16; jj++) {
-            const int j = q * 16 + jj;
-            a[jj] = (r < bs && j < ks)
-                        ? (trans ? A[(long long)(c0 + j) * lda + r0 + r] : A[(long long)(r0 + r) * lda + c0 + j])
-                        : T(0);
+    if (tid == 0) s_fail = 0;
+    for (;;) {
+        __syncthreads();  // the previous block's shared state is no longer read
+        if (tid == 0) s_t = atomicAdd(ctl, 1);
+        __syncthreads();
+        if (s_t >= nb) break;
+        const int b = fwd ? s_t : nb - 1 - s_t, r0 = b * BR, bs = min(BR, n - r0);
+        // the diagonal block and its reciprocal diagonal: no dependence on other blocks
+        for (int idx = tid; idx < bs * bs; idx += blockDim.x) {
+            const int i = idx / bs, j = idx - i * bs;
+            Ds[i * LDD + j] = A[(long long)(r0 + i) * lda + r0 + j];
         }
-        if (tid == 0) {
-            const unsigned long long t0 = global_ns();
-            while (ld_acquire(ctl + 1 + k) == 0) {
-                if (global_ns() - t0 > kBarrierTimeoutNs) {
-                    s_fail = 1;
-                    break;
+        __syncthreads();
+        if (tid < bs) {
+            const T d = Ds[tid * LDD + tid];
+            if (mode != 0 && absT(d) < tiny) atomicCAS(status, 0, RL_ERR_DIV_BY_ZERO);
+            inv[tid] = mode == 0 ? T(1) : T(1) / d;
+        }
+        // thread (row r, quarter q): non-transposed reads A[r][q * 16 + jj] (a thread's 16
+        // columns contiguous), transposed reads A[q * 16 + jj][r] (a warp's rows contiguous)
+        const int r = trans ? (tid & (BR - 1)) : (tid >> 2), q = trans ? (tid >> 6) : (tid & 3);
+        T acc[kSweepRhs];
+    #pragma unroll
+        for (int c = 0; c < kSweepRhs; c++) acc[c] = T(0);
+        const int nk = fwd ? b : nb - 1 - b;  // blocks solved before this one
+        for (int kk = 0; kk < nk; kk++) {
+            const int k = fwd ? kk : nb - 1 - kk, c0 = k * BR, ks = min(BR, n - c0);
+            T a[16];
+    #pragma unroll
+            for (int jj = 0; jj < 16; jj++) {
+                const int j = q * 16 + jj;
+                a[jj] = (r < bs && j < ks)
+                            ? (trans ? A[(long long)(c0 + j) * lda + r0 + r] : A[(long long)(r0 + r) * lda + c0 + j])
+                            : T(0);
+            }
+            if (tid == 0 && !s_fail) {
+                const unsigned long long t0 = global_ns();
+                while (ld_acquire(ctl + 1 + k) == 0) {
+                    if (global_ns() - t0 > kBarrierTimeoutNs) {
+                        s_fail = 1;
+                        break;
+                    }
+                    __nanosleep(100);
                 }
             }
-        }
-        __syncthreads();
-        if (s_fail) break;
-        for (int idx = tid; idx < ks * nrhs; idx += blockDim.x) {
-            const int i = idx / nrhs, c = idx - i * nrhs;
-            xs[i * kSweepRhs + c] = __ldcg(Y + (long long)(c0 + i) * ldy + c);
-        }
-        __syncthreads();
-#pragma unroll
-        for (int jj = 0; jj < 16; jj++) {
-            const int j = q * 16 + jj;
-#pragma unroll
-            for (int c = 0; c < kSweepRhs; c++)
-                if (c < nrhs) acc[c] = fma(a[jj], xs[j * kSweepRhs + c], acc[c]);
-        }
-        __syncthreads();  // xs is refilled for the next block
-    }
-    // sum of the 4 column quarters of each row into xs
-    if (!trans) {
-#pragma unroll
-        for (int c = 0; c < kSweepRhs; c++) {
-            acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 1);
-            acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 2);
-        }
-        if (q == 0)
-#pragma unroll
-            for (int c = 0; c < kSweepRhs; c++) xs[r * kSweepRhs + c] = acc[c];
-        __syncthreads();
-    } else {
-        for (int qq = 0; qq < 4; qq++) {
-            if (q == qq)
-#pragma unroll
-                for (int c = 0; c < kSweepRhs; c++) xs[r * kSweepRhs + c] = (qq ? xs[r * kSweepRhs + c] : T(0)) + acc[c];
             __syncthreads();
-        }
-    }
-    // substitution: warp c solves right-hand side c; lane l holds rows l and l + 32
-    if (warp < nrhs && !s_fail) {
-        const int c = warp;
-        T y[2];
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const int i = lane + 32 * h;
-            T v = T(0);
-            if (i < bs) v = __ldcg(Y + (long long)(r0 + i) * ldy + c) - xs[i * kSweepRhs + c];
-            y[h] = v;
-        }
-        if (fwd) {
-            for (int k = 0; k < bs; k++) {
-                const int h = k >> 5;
-                T xk = __shfl_sync(0xffffffffu, h ? y[1] : y[0], k & 31) * inv[k];
-                if (lane == (k & 31)) {
-                    if (h)
-                        y[1] = xk;
-                    else
-                        y[0] = xk;
-                }
-#pragma unroll
-                for (int hh = 0; hh < 2; hh++) {
-                    const int i = lane + 32 * hh;
-                    if (i > k && i < bs) y[hh] = fma(-Ds[i * LDD + k], xk, y[hh]);
-                }
+            if (s_fail) break;
+            for (int idx = tid; idx < ks * nrhs; idx += blockDim.x) {
+                const int i = idx / nrhs, c = idx - i * nrhs;
+                xs[i * kSweepRhs + c] = __ldcg(Y + (long long)(c0 + i) * ldy + c);
             }
+            __syncthreads();
+    #pragma unroll
+            for (int jj = 0; jj < 16; jj++) {
+                const int j = q * 16 + jj;
+    #pragma unroll
+                for (int c = 0; c < kSweepRhs; c++)
+                    if (c < nrhs) acc[c] = fma(a[jj], xs[j * kSweepRhs + c], acc[c]);
+            }
+            __syncthreads();  // xs is refilled for the next block
+        }
+        // sum of the 4 column quarters of each row into xs
+        if (!trans) {
+    #pragma unroll
+            for (int c = 0; c < kSweepRhs; c++) {
+                acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 1);
+                acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 2);
+            }
+            if (q == 0)
+    #pragma unroll
+                for (int c = 0; c < kSweepRhs; c++) xs[r * kSweepRhs + c] = acc[c];
+            __syncthreads();
         } else {
-            for (int k = bs - 1; k >= 0; k--) {
-                const int h = k >> 5;
-                T xk = __shfl_sync(0xffffffffu, h ? y[1] : y[0], k & 31) * inv[k];
-                if (lane == (k & 31)) {
-                    if (h)
-                        y[1] = xk;
-                    else
-                        y[0] = xk;
-                }
-#pragma unroll
-                for (int hh = 0; hh < 2; hh++) {
-                    const int i = lane + 32 * hh;
-                    if (i < k) y[hh] = fma(-(trans ? Ds[k * LDD + i] : Ds[i * LDD + k]), xk, y[hh]);
-                }
+            for (int qq = 0; qq < 4; qq++) {
+                if (q == qq)
+    #pragma unroll
+                    for (int c = 0; c < kSweepRhs; c++) xs[r * kSweepRhs + c] = (qq ? xs[r * kSweepRhs + c] : T(0)) + acc[c];
+                __syncthreads();
             }
         }
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const int i = lane + 32 * h;
-            if (i < bs) __stcg(Y + (long long)(r0 + i) * ldy + c, y[h]);
+        // substitution: warp c solves right-hand side c; lane l holds rows l and l + 32
+        if (warp < nrhs && !s_fail) {
+            const int c = warp;
+            T y[2];
+    #pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int i = lane + 32 * h;
+                T v = T(0);
+                if (i < bs) v = __ldcg(Y + (long long)(r0 + i) * ldy + c) - xs[i * kSweepRhs + c];
+                y[h] = v;
+            }
+            if (fwd) {
+                for (int k = 0; k < bs; k++) {
+                    const int h = k >> 5;
+                    T xk = __shfl_sync(0xffffffffu, h ? y[1] : y[0], k & 31) * inv[k];
+                    if (lane == (k & 31)) {
+                        if (h)
+                            y[1] = xk;
+                        else
+                            y[0] = xk;
+                    }
+    #pragma unroll
+                    for (int hh = 0; hh < 2; hh++) {
+                        const int i = lane + 32 * hh;
+                        if (i > k && i < bs) y[hh] = fma(-Ds[i * LDD + k], xk, y[hh]);
+                    }
+                }
+            } else {
+                for (int k = bs - 1; k >= 0; k--) {
+                    const int h = k >> 5;
+                    T xk = __shfl_sync(0xffffffffu, h ? y[1] : y[0], k & 31) * inv[k];
+                    if (lane == (k & 31)) {
+                        if (h)
+                            y[1] = xk;
+                        else
+                            y[0] = xk;
+                    }
+    #pragma unroll
+                    for (int hh = 0; hh < 2; hh++) {
+                        const int i = lane + 32 * hh;
+                        if (i < k) y[hh] = fma(-(trans ? Ds[k * LDD + i] : Ds[i * LDD + k]), xk, y[hh]);
+                    }
+                }
+            }
+    #pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int i = lane + 32 * h;
+                if (i < bs) __stcg(Y + (long long)(r0 + i) * ldy + c, y[h]);
+            }
         }
-    }
-    __syncthreads();
-    if (tid == 0) {
-        if (s_fail) atomicCAS(status, 0, RL_ERR_TIMEOUT);
-        __threadfence();
-        st_release(ctl + 1 + b, 1);  // published even after a timeout, so no later block waits forever
+        __syncthreads();
+        if (tid == 0) {
+            if (s_fail) atomicCAS(status, 0, RL_ERR_TIMEOUT);
+            __threadfence();
+            st_release(ctl + 1 + b, 1);  // published even after a timeout, so no later block waits forever
+        }
     }
 }
 
@@ -962,26 +966,78 @@ static __global__ void extract_v_kernel(const T *P, long long lda, int mrows, in
     V[idx] = r > c ? P[(long long)r * lda + c] : (r == c ? T(1) : T(0));
 }
 
-// T factor of H_0 ... H_{kb-1} = I - V T V^T (upper triangular, kb x kb) from the
-// Gram matrix Gm = V^T V and tau: T[j][j] = tau_j, T[0:j, j] = -tau_j T[0:j, 0:j] Gm[0:j, j].
+// Partial Gram matrices of the reflector block V (mrows x kb, row stride kb, kb <= 64):
+// CTA c sums V[r]^T V[r] over its chunk of rows into part[c] (64 x 64). A plain GEMM of
+// this 64 x 64 product over thousands of rows is one tile, one CTA, one long K loop.
+constexpr int kGramRows = 256;  // rows per chunk
 template <class T>
-static __global__ void larft_kernel(const T *Gm, const T *tau, int kb, T *Tm) {
+static __global__ void __launch_bounds__(256) gram_partial_kernel(const T *__restrict__ V, int mrows, int kb,
+                                                                  T *__restrict__ part) {
+    __shared__ T Vs[32][64];
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const int rbeg = blockIdx.x * kGramRows, rend = min(mrows, rbeg + kGramRows);
+    T acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) acc[a][b] = T(0);
+    for (int r0 = rbeg; r0 < rend; r0 += 32) {
+        for (int idx = tid; idx < 32 * 64; idx += 256) {
+            const int r = idx >> 6, c = idx & 63;
+            Vs[r][c] = (r0 + r < rend && c < kb) ? V[(long long)(r0 + r) * kb + c] : T(0);
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int r = 0; r < 32; r++) {
+            T va[4], vb[4];
+#pragma unroll
+            for (int a = 0; a < 4; a++) va[a] = Vs[r][4 * ty + a];
+#pragma unroll
+            for (int b = 0; b < 4; b++) vb[b] = Vs[r][4 * tx + b];
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int b = 0; b < 4; b++) acc[a][b] = fma(va[a], vb[b], acc[a][b]);
+        }
+        __syncthreads();
+    }
+    T *out = part + (size_t)blockIdx.x * 64 * 64;
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) out[(4 * ty + a) * 64 + 4 * tx + b] = acc[a][b];
+}
+
+// T factor of H_0 ... H_{kb-1} = I - V T V^T (upper triangular, kb x kb): the Gram
+// matrix Gm = V^T V is the sum of the nparts partial Gram matrices (added in part order),
+// then T[j][j] = tau_j, T[0:j, j] = -tau_j T[0:j, 0:j] Gm[0:j, j], all in shared memory.
+template <class T>
+static __global__ void __launch_bounds__(256) larft_kernel(const T *part, int nparts, const T *tau, int kb, T *Tm) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T (*G)[65] = reinterpret_cast<T (*)[65]>(smem_raw);  // 64 x 65 each
+    T (*Ts)[65] = G + 64;
     __shared__ T w[64];
     const int t = threadIdx.x;
-    for (int idx = t; idx < kb * kb; idx += blockDim.x) Tm[idx] = T(0);
+    for (int idx = t; idx < 64 * 64; idx += blockDim.x) {
+        T sum = T(0);
+        for (int c = 0; c < nparts; c++) sum += part[(size_t)c * 64 * 64 + idx];
+        G[idx >> 6][idx & 63] = sum;
+        Ts[idx >> 6][idx & 63] = T(0);
+    }
     __syncthreads();
     for (int j = 0; j < kb; j++) {
         const T tj = tau[j];
         if (t < j) {
             T s = T(0);
-            for (int q = t; q < j; q++) s = fma(Tm[t * kb + q], Gm[q * kb + j], s);
+            for (int q = t; q < j; q++) s = fma(Ts[t][q], G[q][j], s);
             w[t] = -tj * s;
         }
         __syncthreads();
-        if (t < j) Tm[t * kb + j] = w[t];
-        if (t == 0) Tm[j * kb + j] = tj;
+        if (t < j) Ts[t][j] = w[t];
+        if (t == 0) Ts[j][j] = tj;
         __syncthreads();
     }
+    for (int idx = t; idx < kb * kb; idx += blockDim.x) Tm[idx] = Ts[idx / kb][idx % kb];
 }
 
 // Identity-like start for first_k_columns: Q (m x k) = I[:, 0:k].

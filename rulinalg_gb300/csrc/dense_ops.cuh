@@ -90,14 +90,22 @@ int probe_cluster(K kern, size_t smem) {
 }
 
 // Cluster size and rows per CTA for a panel of mrows rows of row_bytes each plus `extra`
-// bytes per CTA: as many CTAs as keep at least 32 rows each (up to cmax; the panel's
-// update is bound by each SM's FP64 rate, so every SM added shortens a column), or 0
-// when even cmax CTAs would need more than kClusterSmem bytes each.
+// bytes per CTA: about `target_rows` rows per CTA, clamped to [2, cmax] and to at least
+// the CTAs that the shared memory needs; 0 when even cmax CTAs would need more than
+// kClusterSmem bytes each. FP64 panels take 64 rows per CTA (their row updates run at
+// the SM's FP64 rate, so every SM added shortens a column); FP32 panels take 256, which
+// measured the same alone and keeps clusters small enough to be placed next to the
+// other streams' kernels in the serving loop (16-CTA FP32 clusters halved its
+// throughput: a cluster needs that many SMs of one GPC at once).
+template <class T>
+constexpr int panel_target_rows() {
+    return sizeof(T) == 8 ? 64 : 256;
+}
 constexpr size_t kClusterSmem = 224 * 1024;
-inline int cluster_shape(int mrows, size_t row_bytes, size_t extra, int cmax, int &rows_per) {
+inline int cluster_shape(int mrows, size_t row_bytes, size_t extra, int cmax, int target_rows, int &rows_per) {
     const int cmin = (int)(((size_t)mrows * row_bytes + (kClusterSmem - extra) - 1) / (kClusterSmem - extra));
     if (cmin > cmax || cmax == 0) return 0;
-    int C = std::max(cmin, std::min(cmax, ceil_div(mrows, 32)));
+    int C = std::max(cmin, std::min(cmax, ceil_div(mrows, target_rows)));
     C = std::max(C, 2);
     rows_per = ceil_div(mrows, C);
     return C;
@@ -132,7 +140,7 @@ rl_status lu_panel_cluster(T *P, long long lda, int mrows, int kb, int k0, int *
     static const int cmax = probe_cluster(kern, kClusterSmem);
     const size_t row_bytes = (NB + 1) * sizeof(T), extra = 6 * NB * sizeof(T);
     int rows_per = 0;
-    const int C = cluster_shape(mrows, row_bytes, extra, cmax, rows_per);
+    const int C = cluster_shape(mrows, row_bytes, extra, cmax, panel_target_rows<T>(), rows_per);
     if (C == 0) return RL_OK;
     int tpr = 1;  // threads per row: every thread busy when the CTA holds few rows
     while (tpr < 8 && rows_per * tpr * 2 <= 256) tpr *= 2;
@@ -151,7 +159,7 @@ rl_status qr_panel_cluster(T *P, long long lda, int mrows, int kb, T *tau, cudaS
     static const int cmax = probe_cluster(kern, kClusterSmem);
     const size_t row_bytes = (NB + 1) * sizeof(T), extra = (2 * NB + 2) * sizeof(T);
     int rows_per = 0;
-    const int C = cluster_shape(mrows, row_bytes, extra, cmax, rows_per);
+    const int C = cluster_shape(mrows, row_bytes, extra, cmax, panel_target_rows<T>(), rows_per);
     if (C == 0) return RL_OK;
     RL_TRY(launch_cluster(kern, C, (size_t)rows_per * row_bytes + extra, s, P, lda, mrows, kb, rows_per, tau));
     launched = true;
@@ -235,6 +243,19 @@ rl_status chol_factor_dev(T *A, long long lda, int n, cudaStream_t s, T tiny = E
 
 // Blocked Householder QR with compact-WY trailing updates; nrefl reflectors
 // (min(m, n) for a plain QR; n for the augmented least-squares matrix).
+// Tm of a reflector block V (mrows x kb): partial Gram matrices, then the T recursion.
+template <class T>
+rl_status block_t_factor(const T *V, int mrows, int kb, const T *tau, T *part, int max_parts, T *Tm,
+                         cudaStream_t s) {
+    const int nparts = ceil_div(mrows, kGramRows);
+    if (nparts > max_parts) return RL_ERR_INVALID_ARG;
+    RL_LAUNCH(gram_partial_kernel<T>, nparts, 256, 0, s, V, mrows, kb, part);
+    const size_t smem = 2 * 64 * 65 * sizeof(T);
+    RL_TRY(set_smem(larft_kernel<T>, smem));
+    RL_LAUNCH(larft_kernel<T>, 1, 256, smem, s, part, nparts, tau, kb, Tm);
+    return RL_OK;
+}
+
 template <class T>
 rl_status qr_factor_dev(T *A, long long lda, int m, int n, int nrefl, T *tau, cudaStream_t s) {
     if (nrefl <= 0) return RL_OK;
@@ -242,13 +263,14 @@ rl_status qr_factor_dev(T *A, long long lda, int m, int n, int nrefl, T *tau, cu
     int Gmax, rp;
     panel_geometry<T>(m, Gmax, rp);
     if ((size_t)rp * (NB + 1) * sizeof(T) > 200 * 1024) return RL_ERR_INVALID_ARG;
-    DevBuf<T> part, x0buf, V, Gm, Tm, W1, W2;
+    DevBuf<T> part, x0buf, V, Gp, Tm, W1, W2;
     DevBuf<PanelSync> sync;
     RL_TRY(part.alloc((size_t)2 * Gmax * (1 + NB), s));
     RL_TRY(x0buf.alloc(2, s));
     RL_TRY(sync.alloc(1, s));
     RL_TRY(V.alloc((size_t)m * NB, s));
-    RL_TRY(Gm.alloc(NB * NB, s));
+    const int max_parts = ceil_div(m, kGramRows);
+    RL_TRY(Gp.alloc((size_t)max_parts * 64 * 64, s));
     RL_TRY(Tm.alloc(NB * NB, s));
     RL_TRY(W1.alloc((size_t)NB * std::max(1, n), s));
     RL_TRY(W2.alloc((size_t)NB * std::max(1, n), s));
@@ -274,8 +296,7 @@ rl_status qr_factor_dev(T *A, long long lda, int m, int n, int nrefl, T *tau, cu
         if (n2 <= 0) continue;
         const long long mk = (long long)mrows * kb;
         RL_LAUNCH(extract_v_kernel<T>, (int)((mk + 255) / 256), 256, 0, s, P, lda, mrows, kb, V.p);
-        RL_TRY((gemm<T, true, false>(kb, kb, mrows, T(1), V.p, kb, V.p, kb, T(0), Gm.p, kb, s)));
-        RL_LAUNCH(larft_kernel<T>, 1, 64, 0, s, Gm.p, tk, kb, Tm.p);
+        RL_TRY(block_t_factor<T>(V.p, mrows, kb, tk, Gp.p, max_parts, Tm.p, s));
         T *A2 = P + kb;
         RL_TRY((gemm<T, true, false>(kb, n2, mrows, T(1), V.p, kb, A2, lda, T(0), W1.p, n2, s)));
         RL_TRY((gemm<T, true, false>(kb, n2, kb, T(1), Tm.p, kb, W1.p, n2, T(0), W2.p, n2, s)));
@@ -298,9 +319,10 @@ rl_status qr_first_k_dev(const T *QR, long long lda, int m, int n, const T *tau,
     RL_LAUNCH(eye_kernel<T>, (int)((mk + 255) / 256), 256, 0, s, Q, ldq, m, k);
     const int jmax = std::min(std::min(m, n), k);
     if (jmax <= 0) return RL_OK;
-    DevBuf<T> V, Gm, Tm, W1, W2;
+    DevBuf<T> V, Gp, Tm, W1, W2;
     RL_TRY(V.alloc((size_t)m * NB, s));
-    RL_TRY(Gm.alloc(NB * NB, s));
+    const int max_parts = ceil_div(m, kGramRows);
+    RL_TRY(Gp.alloc((size_t)max_parts * 64 * 64, s));
     RL_TRY(Tm.alloc(NB * NB, s));
     RL_TRY(W1.alloc((size_t)NB * k, s));
     RL_TRY(W2.alloc((size_t)NB * k, s));
@@ -309,8 +331,7 @@ rl_status qr_first_k_dev(const T *QR, long long lda, int m, int n, const T *tau,
         const T *P = QR + (long long)k0 * lda + k0;
         const long long mkb = (long long)mrows * kb;
         RL_LAUNCH(extract_v_kernel<T>, (int)((mkb + 255) / 256), 256, 0, s, P, lda, mrows, kb, V.p);
-        RL_TRY((gemm<T, true, false>(kb, kb, mrows, T(1), V.p, kb, V.p, kb, T(0), Gm.p, kb, s)));
-        RL_LAUNCH(larft_kernel<T>, 1, 64, 0, s, Gm.p, tau + k0, kb, Tm.p);
+        RL_TRY(block_t_factor<T>(V.p, mrows, kb, tau + k0, Gp.p, max_parts, Tm.p, s));
         T *Q2 = Q + (long long)k0 * ldq + k0;
         RL_TRY((gemm<T, true, false>(kb, nc, mrows, T(1), V.p, kb, Q2, ldq, T(0), W1.p, nc, s)));
         RL_TRY((gemm<T, false, false>(kb, nc, kb, T(1), Tm.p, kb, W1.p, nc, T(0), W2.p, nc, s)));
@@ -327,6 +348,39 @@ rl_status tri_solve_dev(const T *A, long long lda, int n, T *Y, long long ldy, i
                         cudaStream_t s, T tiny = Eps<T>::value) {
     if (n <= 0 || nrhs <= 0) return RL_OK;
     constexpr int NB = 64;
+    if (nrhs <= kSweepRhs && g_shared_gpu) {
+        // Few right-hand sides on a shared GPU: per 64-row block a one-CTA diagonal solve
+        // (warp per column) and a warp-per-row GEMV update, all short launches.
+        const int wpb = 8, gridr = std::max(1, std::min(4 * num_sms(), ceil_div(n, wpb)));
+        if (mode == 0 || mode == 1) {
+            for (int b0 = 0; b0 < n; b0 += NB) {
+                const int bs = std::min(NB, n - b0), rest = n - b0 - bs;
+                T *Yb = Y + (long long)b0 * ldy;
+                RL_LAUNCH(trsv_diag_kernel<T>, 1, 256, 0, s, A + (long long)b0 * lda + b0, lda, bs, Yb, ldy, nrhs, mode,
+                          dstatus, tiny);
+                if (rest > 0)
+                    RL_LAUNCH(gemv_update_kernel<T>, std::min(gridr, ceil_div(rest, wpb)), 32 * wpb, 0, s,
+                              A + (long long)(b0 + bs) * lda + b0, lda, rest, bs, Yb, ldy, Yb + (long long)bs * ldy,
+                              nrhs, false);
+            }
+        } else {
+            for (int b1 = n; b1 > 0; b1 -= NB) {
+                const int b0 = std::max(0, b1 - NB), bs = b1 - b0;
+                T *Yb = Y + (long long)b0 * ldy;
+                RL_LAUNCH(trsv_diag_kernel<T>, 1, 256, 0, s, A + (long long)b0 * lda + b0, lda, bs, Yb, ldy, nrhs, mode,
+                          dstatus, tiny);
+                if (b0 > 0) {
+                    if (mode == 2)
+                        RL_LAUNCH(gemv_update_kernel<T>, std::min(gridr, ceil_div(b0, wpb)), 32 * wpb, 0, s, A + b0, lda,
+                                  b0, bs, Yb, ldy, Y, nrhs, false);
+                    else
+                        RL_LAUNCH(gemv_update_kernel<T>, ceil_div(b0, 256), 256, 0, s, A + (long long)b0 * lda, lda, b0,
+                                  bs, Yb, ldy, Y, nrhs, true);
+                }
+            }
+        }
+        return RL_OK;
+    }
     if (nrhs <= kSweepRhs) {
         // Few right-hand sides: the whole solve in one launch (trsv_sweep_kernel); a GEMM
         // tile per block would waste all but nrhs of its columns.
@@ -334,7 +388,8 @@ rl_status tri_solve_dev(const T *A, long long lda, int n, T *Y, long long ldy, i
         DevBuf<int> ctl;
         RL_TRY(ctl.alloc(1 + nb, s));
         RL_TRY_CUDA(cudaMemsetAsync(ctl.p, 0, sizeof(int) * (1 + nb), s));
-        RL_LAUNCH(trsv_sweep_kernel<T>, nb, 256, 0, s, A, lda, n, Y, ldy, nrhs, mode, ctl.p, dstatus, tiny);
+        RL_LAUNCH(trsv_sweep_kernel<T>, std::min(nb, kSweepCtas), 256, 0, s, A, lda, n, Y, ldy, nrhs, mode, ctl.p, dstatus,
+                  tiny);
         return RL_OK;
     }
     const int gr = ceil_div(nrhs, kTrsmCols);

@@ -47,7 +47,7 @@ __device__ __forceinline__ void lds4<double>(const double *p, double (&o)[4]) {
 template <class T, bool TA, bool TB, bool LOWER>
 __global__ void __launch_bounds__((GemmCfg<T>::BM / GemmCfg<T>::TM) * (GemmCfg<T>::BN / GemmCfg<T>::TN))
     gemm_kernel(int m, int n, int k, T alpha, const T *__restrict__ A, long long lda, const T *__restrict__ B,
-                long long ldb, T beta, T *__restrict__ C, long long ldc) {
+                long long ldb, T beta, T *__restrict__ C, long long ldc, int kslice, long long zstride) {
     constexpr int BM = GemmCfg<T>::BM, BN = GemmCfg<T>::BN, BK = GemmCfg<T>::BK;
     constexpr int TM = GemmCfg<T>::TM, TN = GemmCfg<T>::TN;
     constexpr int NTX = BN / TN, NTY = BM / TM, NT = NTX * NTY;
@@ -58,6 +58,13 @@ __global__ void __launch_bounds__((GemmCfg<T>::BM / GemmCfg<T>::TM) * (GemmCfg<T
     __shared__ __align__(16) T As[2][BK][BM];
     __shared__ __align__(16) T Bs[2][BK][BN];
 
+    if (gridDim.z > 1) {  // split K: slice z of the reduction into its own partial C
+        const int kz = blockIdx.z * kslice;
+        k = max(0, min(kslice, k - kz));
+        A += TA ? (long long)kz * lda : kz;
+        B += TB ? kz : (long long)kz * ldb;
+        C += blockIdx.z * zstride;
+    }
     const int tid = threadIdx.x;
     const int tx = tid % NTX, ty = tid / NTX;
     const int row0 = blockIdx.y * BM, col0 = blockIdx.x * BN;
@@ -188,19 +195,42 @@ __global__ void __launch_bounds__((GemmCfg<T>::BM / GemmCfg<T>::TM) * (GemmCfg<T
 
 // Launches C = alpha * op(A) op(B) + beta * C on `stream`. FP32 products with at least
 // a 128 x 128 tile's worth of C and K >= 256 go to the tcgen05 kernel (gemm_tc.cuh).
+// A product with fewer tiles than SMs and a long K (the V^T A2 and V^T V products of a
+// Householder block, K = the panel height) is split along K into partial tiles that
+// run at once, then added in slice order.
 template <class T, bool TA, bool TB, bool LOWER = false>
 rl_status gemm(int m, int n, int k, T alpha, const T *A, long long lda, const T *B, long long ldb, T beta, T *C,
                long long ldc, cudaStream_t stream) {
     if (m <= 0 || n <= 0) return RL_OK;
-    if constexpr (std::is_same<T, float>::value) {  // FP32 with enough work: tensor cores (3xTF32)
-        if (sgemm_tc_eligible(m, n, k))
-            return sgemm_tc<TA, TB>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, LOWER, stream);
-    }
-    constexpr int BM = GemmCfg<T>::BM, BN = GemmCfg<T>::BN;
+    constexpr int BM = GemmCfg<T>::BM, BN = GemmCfg<T>::BN, BK = GemmCfg<T>::BK;
     constexpr int NT = (BM / GemmCfg<T>::TM) * (BN / GemmCfg<T>::TN);
     dim3 grid((n + BN - 1) / BN, (m + BM - 1) / BM);
-    RL_LAUNCH((gemm_kernel<T, TA, TB, LOWER>), grid, NT, 0, stream, m, n, k, alpha, A, lda, B, ldb, beta, C,
-              ldc);
+    const int tiles = (int)(grid.x * grid.y), sms = num_sms();
+    if constexpr (std::is_same<T, float>::value) {  // FP32 with enough work: tensor cores (3xTF32)
+        if (sgemm_tc_eligible(m, n, k)) {
+            const int tc_tiles = ceil_div(n, tc::BN) * ceil_div(m, tc::BM);
+            int ks = 1;
+            if (!LOWER && tc_tiles < sms / 2 && k >= 1024) ks = std::min({16, ceil_div(sms, tc_tiles), k / 256});
+            return sgemm_tc<TA, TB>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, LOWER, stream, ks);
+        }
+    }
+    int ksplit = 1;
+    if (!LOWER && tiles < sms && k >= 1024) ksplit = std::min({16, ceil_div(2 * sms, tiles), k / 256});
+    if (ksplit > 1) {
+        const int kslice = ceil_div(ceil_div(k, ksplit), BK) * BK;
+        ksplit = ceil_div(k, kslice);
+        const long long zstride = (long long)m * n;
+        DevBuf<T> part;
+        RL_TRY(part.alloc((size_t)ksplit * zstride, stream));
+        grid.z = ksplit;
+        RL_LAUNCH((gemm_kernel<T, TA, TB, LOWER>), grid, NT, 0, stream, m, n, k, T(1), A, lda, B, ldb, T(0), part.p, (long long)n,
+                  kslice, zstride);
+        RL_LAUNCH(splitk_reduce_kernel<T>, std::min(4 * sms, ceil_div(zstride, 256)), 256, 0, stream, m, n, ksplit, alpha,
+                  part.p, beta, C, ldc);
+        return RL_OK;
+    }
+    RL_LAUNCH((gemm_kernel<T, TA, TB, LOWER>), grid, NT, 0, stream, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, k,
+              0ll);
     return RL_OK;
 }
 

@@ -171,7 +171,8 @@ static __global__ void split_transpose_kernel(const float *__restrict__ B, long 
 static __global__ void __launch_bounds__(tc::THREADS, 1)
     sgemm_tma_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUtensorMap tAl,
                      const __grid_constant__ CUtensorMap tBh, const __grid_constant__ CUtensorMap tBl, int m, int n,
-                     int kp, float alpha, float beta, float *__restrict__ C, long long ldc, int lower, int *err) {
+                     int kp, float alpha, float beta, float *__restrict__ C, long long ldc, int lower, int *err,
+                     int kc_per, long long zstride) {
     using namespace tc;
     // lower: only the elements on or below the diagonal are written (the SYRK form);
     // tiles wholly above it do nothing
@@ -186,7 +187,10 @@ static __global__ void __launch_bounds__(tc::THREADS, 1)
     __shared__ int s_fail;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int row0 = blockIdx.y * BM, col0 = blockIdx.x * BN;
-    const int nk = kp / BK;
+    // split K: slice z covers the K chunks [c_begin, c_begin + nk) into its own partial C
+    const int c_begin = blockIdx.z * kc_per;
+    const int nk = max(0, min(kp / BK, c_begin + kc_per) - c_begin);
+    C += blockIdx.z * zstride;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
@@ -217,10 +221,11 @@ static __global__ void __launch_bounds__(tc::THREADS, 1)
             }
             unsigned char *st = smem + s * STAGE_BYTES;
             mbar_expect_tx(&full[s], STAGE_BYTES);
-            tma_load_2d(st, &tAh, c * BK, row0, &full[s]);
-            tma_load_2d(st + TILE_BYTES, &tAl, c * BK, row0, &full[s]);
-            tma_load_2d(st + 2 * TILE_BYTES, &tBh, c * BK, col0, &full[s]);
-            tma_load_2d(st + 3 * TILE_BYTES, &tBl, c * BK, col0, &full[s]);
+            const int x = (c_begin + c) * BK;
+            tma_load_2d(st, &tAh, x, row0, &full[s]);
+            tma_load_2d(st + TILE_BYTES, &tAl, x, row0, &full[s]);
+            tma_load_2d(st + 2 * TILE_BYTES, &tBh, x, col0, &full[s]);
+            tma_load_2d(st + 3 * TILE_BYTES, &tBl, x, col0, &full[s]);
         }
     } else if (warp == 1 && lane == 0) {  // MMA issuer
         constexpr uint32_t idesc = idesc_tf32(BM, BN);
@@ -320,12 +325,30 @@ inline rl_status make_tile_map(CUtensorMap &map, const float *base, int rows, in
     return r == CUDA_SUCCESS ? RL_OK : RL_ERR_CUDA;
 }
 
+// C = alpha * sum_z P[z] + beta * C (m x n; P[z] packed with row stride n), in z order.
+template <class T>
+__global__ void splitk_reduce_kernel(int m, int n, int nz, T alpha, const T *__restrict__ P, T beta, T *__restrict__ C,
+                                     long long ldc) {
+    const long long total = (long long)m * n;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        T sum = T(0);
+        for (int z = 0; z < nz; z++) sum += P[z * total + e];
+        const int i = (int)(e / n), j = (int)(e - (long long)i * n);
+        T *cp = C + (long long)i * ldc + j;
+        T v = alpha * sum;
+        if (beta != T(0)) v = fma(beta, *cp, v);
+        *cp = v;
+    }
+}
+
 // C = alpha op(A) op(B) + beta C on the tensor cores (3xTF32); any strides, any
 // alignment. op(A) = A (m x k, A[i * lda + p]) or A^T (A[p * lda + i]); op(B) = B (k x n,
 // B[p * ldb + j]) or B^T (B[j * ldb + p]). The split kernels repack both operands K-major.
+// ksplit > 1 (not with `lower`) runs K in that many slices at once into partial tiles,
+// added in slice order afterwards: for products with few output tiles and a long K.
 template <bool TA, bool TB>
 rl_status sgemm_tc(int m, int n, int k, float alpha, const float *A, long long lda, const float *B, long long ldb,
-                   float beta, float *C, long long ldc, bool lower, cudaStream_t s) {
+                   float beta, float *C, long long ldc, bool lower, cudaStream_t s, int ksplit = 1) {
     static const cudaError_t attr =
         cudaFuncSetAttribute(sgemm_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
     RL_TRY_CUDA(attr);
@@ -355,9 +378,22 @@ rl_status sgemm_tc(int m, int n, int k, float alpha, const float *A, long long l
     RL_TRY(make_tile_map(mBl, Bl.p, n, kp));
     int *err = nullptr;
     RL_TRY_CUDA(cudaGetSymbolAddress(reinterpret_cast<void **>(&err), g_sgemm_tc_err));
-    const dim3 grid((n + tc::BN - 1) / tc::BN, (m + tc::BM - 1) / tc::BM);
+    dim3 grid((n + tc::BN - 1) / tc::BN, (m + tc::BM - 1) / tc::BM);
+    const int nkc = kp / tc::BK;
+    if (ksplit > 1 && !lower) {
+        const int kc_per = (nkc + ksplit - 1) / ksplit;
+        grid.z = (nkc + kc_per - 1) / kc_per;
+        const long long zstride = (long long)m * n;
+        DevBuf<float> part;
+        RL_TRY(part.alloc((size_t)grid.z * zstride, s));
+        RL_LAUNCH(sgemm_tma_kernel, grid, tc::THREADS, tc::SMEM_BYTES, s, mAh, mAl, mBh, mBl, m, n, kp, 1.f, 0.f, part.p,
+                  (long long)n, 0, err, kc_per, zstride);
+        RL_LAUNCH(splitk_reduce_kernel<float>, (int)std::min<long long>(4LL * num_sms(), (zstride + 255) / 256), 256, 0, s,
+                  m, n, (int)grid.z, alpha, part.p, beta, C, ldc);
+        return RL_OK;
+    }
     RL_LAUNCH(sgemm_tma_kernel, grid, tc::THREADS, tc::SMEM_BYTES, s, mAh, mAl, mBh, mBl, m, n, kp, alpha, beta, C,
-              ldc, lower ? 1 : 0, err);
+              ldc, lower ? 1 : 0, err, nkc, 0ll);
     return RL_OK;
 }
 

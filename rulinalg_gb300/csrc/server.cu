@@ -354,6 +354,7 @@ struct Worker {
     }
 
     void loop() {
+        g_shared_gpu = true;  // this thread's solves run next to the other workers'
         for (;;) {
             std::vector<Req *> job;
             {

@@ -75,6 +75,23 @@ def test_sgemm_tensor_core_elementwise(gpu, m, k, n):
     assert np.all(np.abs(got - ref) <= bound), np.max(np.abs(got - ref) / bound)
 
 
+@pytest.mark.parametrize("m,k,n,dtype", [(128, 4096, 128, np.float32), (64, 3000, 300, np.float32),
+                                         (50, 5000, 60, np.float32), (64, 4096, 64, np.float64),
+                                         (100, 3000, 130, np.float64)])
+def test_gemm_split_k(gpu, m, k, n, dtype):
+    """Products with few output tiles and a long K run as K slices at once (tensor-core
+    and SIMT paths, ragged slices): every element within the dot-product bound of the
+    type, 2 k eps (|A| |B|)."""
+    rng = np.random.default_rng(m + k + n)
+    a = rng.standard_normal((m, k)).astype(dtype)
+    b = rng.standard_normal((k, n)).astype(dtype)
+    got = gpu.mat_mul(a, b).astype(np.float64)
+    a64, b64 = a.astype(np.float64), b.astype(np.float64)
+    eps = U32 if dtype == np.float32 else U64
+    bound = 2 * k * eps * (np.abs(a64) @ np.abs(b64))
+    assert np.all(np.abs(got - a64 @ b64) <= bound), np.max(np.abs(got - a64 @ b64) / bound)
+
+
 def test_gemm_k_zero_and_empty(gpu):
     c = gpu.mat_mul(np.zeros((3, 0)), np.zeros((0, 4)))
     assert c.shape == (3, 4) and not c.any()
