@@ -138,7 +138,10 @@ inline rl_status gmres_ir(const double *A, long long lda, int n, const Minv &M, 
             ok = true;
             return RL_OK;
         }
-        if (outer == outer_max - 1 || !(rn <= 0.1 * prev_rn)) return RL_OK;  // out of budget, or no progress
+        if (outer == outer_max - 1 || !(rn <= 0.1 * prev_rn)) {  // out of budget, or no progress:
+            ok = out.berr <= 10.0 * n * kU;                        // accept within the 10 n u bound
+            return RL_OK;
+        }
         prev_rn = rn;
         // z = M^-1 r -> V[0] = z / ||z||, g = (||z||, 0, ...)
         RL_TRY(M.apply(r.p, w.p, s));
@@ -366,7 +369,7 @@ struct MixedFactor {
         RL_TRY(colnorm_dev(B, ldb, n, nrhs, bn_b, s));
         const long long tot = (long long)n * nrhs;
         const int ge = (int)std::min<long long>(4 * num_sms(), (tot + 255) / 256);
-        std::vector<int> conv(nrhs, 0);
+        std::vector<int> conv(nrhs, 0), near(nrhs, 0);
         std::vector<double> prev(nrhs, INFINITY), bnorm(nrhs, 0.0);
         // x0 = M^-1 b
         RL_LAUNCH(scale_to_f32_kernel, ge, 256, 0, s, B, ldb, n, nrhs, bn_b, W.p, (long long)nrhs);
@@ -395,6 +398,7 @@ struct MixedFactor {
                 conv[c] = rn <= std::sqrt((double)n) * kU * anorm * xn;
                 const double den = anorm * xn + bnorm[c];
                 berr = std::max(berr, den > 0 ? rn / den : 0.0);
+                near[c] = rn <= 10.0 * n * kU * den;
                 // diverging (a growing residual) or stalling (not halving after two steps)
                 if (!conv[c] && ((it >= 1 && rn > prev[c]) || (it >= 2 && rn > 0.5 * prev[c]))) stalled = true;
                 // the first correction made things worse: the FP32 factor is too far off
@@ -407,7 +411,13 @@ struct MixedFactor {
             }
             out.berr = berr;
             out.iters = it;
-            if (all || stalled || it >= 10) break;
+            // LAPACK dsgesv's test and step limit (30); a column that stalls or runs out
+            // of steps is accepted within the 10 n u backward-error bound (the batched
+            // solver's rule), where a large n's residual floor can sit above the test
+            if (all || stalled || it >= 30) {
+                for (int c = 0; c < nrhs; c++) conv[c] |= near[c];
+                break;
+            }
             RL_TRY_CUDA(cudaMemcpyAsync(active.p, act.data(), nrhs * sizeof(int), cudaMemcpyHostToDevice, s));
             RL_LAUNCH(scale_to_f32_kernel, ge, 256, 0, s, R.p, (long long)nrhs, n, nrhs, rn_b, W.p, (long long)nrhs);
             RL_TRY(precond_solve(F, n, kind, ipiv, W.p, nrhs, nrhs, dstatus.p, s));
