@@ -36,13 +36,20 @@ struct rl_batch_plan {
     void *h_a = nullptr, *h_b = nullptr, *h_x = nullptr;
     int *h_info = nullptr, *h_iters = nullptr;
     double *h_berr = nullptr;
-    // host-pointer pipeline: contiguous chunks of systems, each copied on its own stream
-    // while the previous chunk is solved (largest-first order within each chunk)
+    // host-pointer pipeline: contiguous chunks of systems copied one after another on the
+    // copy stream while ONE launch solves them in chunk order (largest-first within each
+    // chunk), each CTA waiting on the chunk's arrival flag. In the device copies every
+    // chunk starts on a 256-byte boundary (a_shift / b_shift elements added to the
+    // offsets), so no cache sector holds bytes of two chunks: an SM that read the end of
+    // chunk c - 1 cannot have cached bytes of chunk c before they arrived.
     std::vector<int> chunk_first, chunk_count;
-    int *d_corder = nullptr, *d_ccounters = nullptr;
+    std::vector<long long> a_shift, b_shift;
+    long long a_total_h = 0, b_total_h = 0;
+    int *d_corder = nullptr, *d_ccounters = nullptr, *d_gate = nullptr, *d_gate_pos = nullptr;
+    long long *d_aoff_h = nullptr, *d_boff_h = nullptr;
+    int *h_one = nullptr;  // pinned host 1, copied into d_gate[c] after chunk c
     cudaStream_t copy = nullptr;
     cudaEvent_t ev_start = nullptr;
-    std::vector<cudaEvent_t> ev_chunk;
 
     std::mutex mu;
 };
@@ -131,20 +138,21 @@ rl_status run_plan(rl_batch_plan *p, const TI *a, const TI *b, TI *x, int *info,
     return RL_OK;
 }
 
+// The host-path launch: the main pass over all chunks, gated per chunk, then (mixed) the
+// FP64 pass over the systems it handed on.
 template <class TI, class TF, bool MIXED>
-rl_status launch_chunk(rl_batch_plan *p, int c, const TI *a, const TI *b, TI *x, cudaStream_t s) {
-    const int first = p->chunk_first[c], cnt = p->chunk_count[c];
-    int *ctr = p->d_ccounters + 4 * c;
+rl_status launch_gated(rl_batch_plan *p, const TI *a, const TI *b, TI *x, cudaStream_t s) {
+    int *ctr = p->d_ccounters;
     BatchDesc d{};
-    d.count = cnt;
+    d.count = (int)p->count;
     d.count_dev = nullptr;
-    d.order = p->d_corder + first;
+    d.order = p->d_corder;
     d.n = p->d_n;
     d.kind = p->d_kind;
-    d.a_off = p->d_aoff;
-    d.b_off = p->d_boff;
+    d.a_off = p->d_aoff_h;
+    d.b_off = p->d_boff_h;
     d.next = ctr;
-    d.fb_list = p->d_fb_list + first;
+    d.fb_list = p->d_fb_list;
     d.fb_count = ctr + 1;
     d.work = p->d_work;
     d.work_stride = p->work_stride;
@@ -153,8 +161,17 @@ rl_status launch_chunk(rl_batch_plan *p, int c, const TI *a, const TI *b, TI *x,
     d.berr = p->h_berr;
     d.iters_tag = 0;
     d.max_iters = 30;
-    d.warp_small = 1;  // the order is largest-cost first
-    RL_LAUNCH((batch_solve_kernel<TI, TF, MIXED>), std::min(p->grid, cnt), CTA_THREADS, p->smem, s, d, a, b, x);
+    d.warp_small = 1;  // largest-cost first within each chunk: the last chunk's tail
+    d.warp_from = p->chunk_first.back();
+    d.gate = p->d_gate;
+    d.gate_pos = p->d_gate_pos;
+    d.gate_n = (int)p->chunk_first.size();
+    d.gate_err = ctr + 3;
+    static const cudaError_t attr = cudaFuncSetAttribute(batch_solve_kernel<TI, TF, MIXED, true>,
+                                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem);
+    RL_TRY_CUDA(attr);
+    RL_LAUNCH((batch_solve_kernel<TI, TF, MIXED, true>), std::min<long long>(p->grid, p->count), CTA_THREADS, p->smem,
+              s, d, a, b, x);
     if (MIXED) {
         BatchDesc f = d;
         f.count = 0;
@@ -164,63 +181,75 @@ rl_status launch_chunk(rl_batch_plan *p, int c, const TI *a, const TI *b, TI *x,
         f.work = p->d_work64;
         f.iters_tag = -1;
         f.warp_small = 0;  // the fallback list is in arrival order
-        RL_LAUNCH((batch_solve_kernel<TI, double, false>), std::min(p->grid64, cnt), CTA_THREADS, p->smem64, s, f, a,
-                  b, x);
+        f.warp_from = 0;
+        f.gate_n = 0;      // every chunk is in by the time it runs
+        RL_LAUNCH((batch_solve_kernel<TI, double, false>), std::min<long long>(p->grid64, p->count), CTA_THREADS,
+                  p->smem64, s, f, a, b, x);
     }
     return RL_OK;
 }
 
-// Host buffers in, host buffers out. The systems go in contiguous chunks: chunk c's
-// matrices and vectors are copied on the plan's copy stream while chunk c - 1 is solved
-// on the caller's stream, so the transfer and the solve overlap.
+// Host buffers in, host buffers out. The systems go in contiguous chunks copied on the
+// plan's copy stream, each followed by its arrival flag; the solve is one launch on the
+// caller's stream that takes chunk c's systems once its flag is set, so the transfer
+// and the solve overlap with no drain of the GPU between chunks.
 template <class TI>
 rl_status solve_host(rl_batch_plan *p, const TI *a, const TI *b, TI *x, int32_t *info, int32_t *iters,
                      double *berr) {
     cudaStream_t s = cudaStreamPerThread;
+    if (p->count == 0) return RL_OK;
     if (!p->h_a) {
-        RL_TRY_CUDA(cudaMalloc(&p->h_a, std::max<long long>(1, p->a_total) * sizeof(TI)));
-        RL_TRY_CUDA(cudaMalloc(&p->h_b, std::max<long long>(1, p->b_total) * sizeof(TI)));
-        RL_TRY_CUDA(cudaMalloc(&p->h_x, std::max<long long>(1, p->b_total) * sizeof(TI)));
+        RL_TRY_CUDA(cudaMalloc(&p->h_a, std::max<long long>(1, p->a_total_h) * sizeof(TI)));
+        RL_TRY_CUDA(cudaMalloc(&p->h_b, std::max<long long>(1, p->b_total_h) * sizeof(TI)));
+        RL_TRY_CUDA(cudaMalloc(&p->h_x, std::max<long long>(1, p->b_total_h) * sizeof(TI)));
         RL_TRY_CUDA(cudaMalloc(&p->h_info, std::max<size_t>(1, p->count) * sizeof(int)));
         RL_TRY_CUDA(cudaMalloc(&p->h_iters, std::max<size_t>(1, p->count) * sizeof(int)));
         RL_TRY_CUDA(cudaMalloc(&p->h_berr, std::max<size_t>(1, p->count) * sizeof(double)));
+        RL_TRY_CUDA(cudaMallocHost(&p->h_one, sizeof(int)));
+        *p->h_one = 1;
         RL_TRY_CUDA(cudaStreamCreateWithFlags(&p->copy, cudaStreamNonBlocking));
         RL_TRY_CUDA(cudaEventCreateWithFlags(&p->ev_start, cudaEventDisableTiming));
-        p->ev_chunk.assign(p->chunk_first.size(), nullptr);
-        for (auto &e : p->ev_chunk) RL_TRY_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
     TI *da = static_cast<TI *>(p->h_a), *db = static_cast<TI *>(p->h_b), *dx = static_cast<TI *>(p->h_x);
     const int nch = (int)p->chunk_first.size();
-    RL_TRY_CUDA(cudaMemsetAsync(p->d_ccounters, 0, 4 * std::max(1, nch) * sizeof(int), s));
-    RL_TRY_CUDA(cudaEventRecord(p->ev_start, s));  // earlier work on the buffers comes first
+    RL_TRY_CUDA(cudaMemsetAsync(p->d_ccounters, 0, 4 * sizeof(int), s));
+    RL_TRY_CUDA(cudaMemsetAsync(p->d_gate, 0, nch * sizeof(int), s));
+    RL_TRY_CUDA(cudaEventRecord(p->ev_start, s));  // earlier work on the buffers, and the resets, first
     RL_TRY_CUDA(cudaStreamWaitEvent(p->copy, p->ev_start, 0));
     for (int c = 0; c < nch; c++) {
         const int first = p->chunk_first[c], end = first + p->chunk_count[c];
         const long long a0 = p->a_off[first], a1 = end < (int)p->count ? p->a_off[end] : p->a_total;
         const long long b0 = p->b_off[first], b1 = end < (int)p->count ? p->b_off[end] : p->b_total;
         if (a1 > a0)
-            RL_TRY_CUDA(cudaMemcpyAsync(da + a0, a + a0, (a1 - a0) * sizeof(TI), cudaMemcpyHostToDevice, p->copy));
+            RL_TRY_CUDA(cudaMemcpyAsync(da + a0 + p->a_shift[c], a + a0, (a1 - a0) * sizeof(TI), cudaMemcpyHostToDevice,
+                                        p->copy));
         if (b1 > b0)
-            RL_TRY_CUDA(cudaMemcpyAsync(db + b0, b + b0, (b1 - b0) * sizeof(TI), cudaMemcpyHostToDevice, p->copy));
-        RL_TRY_CUDA(cudaEventRecord(p->ev_chunk[c], p->copy));
-        RL_TRY_CUDA(cudaStreamWaitEvent(s, p->ev_chunk[c], 0));
-        rl_status st;
-        if (std::is_same<TI, float>::value)
-            st = launch_chunk<float, float, false>(p, c, (const float *)da, (const float *)db, (float *)dx, s);
-        else if (p->precision == RL_PREC_MIXED)
-            st = launch_chunk<double, float, true>(p, c, (const double *)da, (const double *)db, (double *)dx, s);
-        else
-            st = launch_chunk<double, double, false>(p, c, (const double *)da, (const double *)db, (double *)dx, s);
-        RL_TRY(st);
+            RL_TRY_CUDA(cudaMemcpyAsync(db + b0 + p->b_shift[c], b + b0, (b1 - b0) * sizeof(TI), cudaMemcpyHostToDevice,
+                                        p->copy));
+        RL_TRY_CUDA(cudaMemcpyAsync(p->d_gate + c, p->h_one, sizeof(int), cudaMemcpyHostToDevice, p->copy));
     }
-    if (p->b_total) RL_TRY_CUDA(cudaMemcpyAsync(x, dx, p->b_total * sizeof(TI), cudaMemcpyDeviceToHost, s));
-    if (info && p->count) RL_TRY_CUDA(cudaMemcpyAsync(info, p->h_info, p->count * sizeof(int), cudaMemcpyDeviceToHost, s));
-    if (iters && p->count)
-        RL_TRY_CUDA(cudaMemcpyAsync(iters, p->h_iters, p->count * sizeof(int), cudaMemcpyDeviceToHost, s));
-    if (berr && p->count)
-        RL_TRY_CUDA(cudaMemcpyAsync(berr, p->h_berr, p->count * sizeof(double), cudaMemcpyDeviceToHost, s));
+    rl_status st;
+    if (std::is_same<TI, float>::value)
+        st = launch_gated<float, float, false>(p, (const float *)da, (const float *)db, (float *)dx, s);
+    else if (p->precision == RL_PREC_MIXED)
+        st = launch_gated<double, float, true>(p, (const double *)da, (const double *)db, (double *)dx, s);
+    else
+        st = launch_gated<double, double, false>(p, (const double *)da, (const double *)db, (double *)dx, s);
+    RL_TRY(st);
+    for (int c = 0; c < nch; c++) {
+        const int first = p->chunk_first[c], end = first + p->chunk_count[c];
+        const long long b0 = p->b_off[first], b1 = end < (int)p->count ? p->b_off[end] : p->b_total;
+        if (b1 > b0)
+            RL_TRY_CUDA(cudaMemcpyAsync(x + b0, dx + b0 + p->b_shift[c], (b1 - b0) * sizeof(TI), cudaMemcpyDeviceToHost,
+                                        s));
+    }
+    if (info) RL_TRY_CUDA(cudaMemcpyAsync(info, p->h_info, p->count * sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (iters) RL_TRY_CUDA(cudaMemcpyAsync(iters, p->h_iters, p->count * sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (berr) RL_TRY_CUDA(cudaMemcpyAsync(berr, p->h_berr, p->count * sizeof(double), cudaMemcpyDeviceToHost, s));
+    int gate_err = 0;
+    RL_TRY_CUDA(cudaMemcpyAsync(&gate_err, p->d_ccounters + 3, sizeof(int), cudaMemcpyDeviceToHost, s));
     RL_TRY_CUDA(cudaStreamSynchronize(s));
-    return RL_OK;
+    return gate_err ? RL_ERR_TIMEOUT : RL_OK;
 }
 
 template <class T>
@@ -265,10 +294,12 @@ rl_status plan_init(rl_batch_plan *p, size_t count, const int32_t *n, const uint
     RL_TRY(upload(p->d_aoff, p->a_off, s));
     RL_TRY(upload(p->d_boff, p->b_off, s));
     RL_TRY(upload(p->d_order, order, s));
-    // Host-path chunks: up to 8 contiguous ranges of about equal matrix bytes, each with
-    // its own largest-first order.
+    // Host-path chunks: up to 32 contiguous ranges of about equal matrix bytes, each with
+    // its own largest-first order. Small chunks shorten both ends of the pipeline (the
+    // solve starts after the first chunk's copy and ends a chunk's solve after the last
+    // one's); with one gated launch there is no drain between chunks to pay for them.
     {
-        const int want = (int)std::min<size_t>(8, std::max<size_t>(1, count));
+        const int want = (int)std::min<size_t>(32, std::max<size_t>(1, count));
         std::vector<int> corder;
         corder.reserve(count);
         size_t i = 0;
@@ -286,6 +317,35 @@ rl_status plan_init(rl_batch_plan *p, size_t count, const int32_t *n, const uint
         }
         RL_TRY(upload(p->d_corder, corder, s));
         RL_TRY_CUDA(cudaMalloc(&p->d_ccounters, 4 * std::max<size_t>(1, p->chunk_first.size()) * sizeof(int)));
+        // device layout of the host path: chunk starts rounded up to 64 elements (256
+        // bytes in FP32, 512 in FP64)
+        const int nch = (int)p->chunk_first.size();
+        auto round64 = [](long long v) { return (v + 63) & ~63LL; };
+        p->a_shift.assign(nch, 0);
+        p->b_shift.assign(nch, 0);
+        long long a_end = 0, b_end = 0;
+        std::vector<long long> aoff_h(count), boff_h(count);
+        std::vector<int> gate_pos(nch + 1, (int)count);
+        for (int c = 0; c < nch; c++) {
+            const int first = p->chunk_first[c], end = first + p->chunk_count[c];
+            const long long a0 = p->a_off[first], a1 = end < (int)count ? p->a_off[end] : p->a_total;
+            const long long b0 = p->b_off[first], b1 = end < (int)count ? p->b_off[end] : p->b_total;
+            p->a_shift[c] = round64(a_end) - a0;
+            p->b_shift[c] = round64(b_end) - b0;
+            a_end = a1 + p->a_shift[c];
+            b_end = b1 + p->b_shift[c];
+            for (int k = first; k < end; k++) {
+                aoff_h[k] = p->a_off[k] + p->a_shift[c];
+                boff_h[k] = p->b_off[k] + p->b_shift[c];
+            }
+            gate_pos[c] = first;
+        }
+        p->a_total_h = a_end;
+        p->b_total_h = b_end;
+        RL_TRY(upload(p->d_aoff_h, aoff_h, s));
+        RL_TRY(upload(p->d_boff_h, boff_h, s));
+        RL_TRY(upload(p->d_gate_pos, gate_pos, s));
+        RL_TRY_CUDA(cudaMalloc(&p->d_gate, std::max(1, nch) * sizeof(int)));
     }
     RL_TRY_CUDA(cudaMalloc(&p->d_counters, 4 * sizeof(int)));
     RL_TRY_CUDA(cudaMalloc(&p->d_fb_list, std::max<size_t>(1, count) * sizeof(int)));
@@ -319,13 +379,12 @@ void plan_free(rl_batch_plan *p) {
     if (p->cap) cudaStreamDestroy(p->cap);
     if (p->copy) cudaStreamDestroy(p->copy);
     if (p->ev_start) cudaEventDestroy(p->ev_start);
-    for (cudaEvent_t e : p->ev_chunk)
-        if (e) cudaEventDestroy(e);
-    void *ptrs[] = {p->d_n, p->d_order, p->d_counters, p->d_fb_list, p->d_kind, p->d_aoff, p->d_boff, p->d_work,
-                    p->d_work64, p->h_a, p->h_b, p->h_x, p->h_info, p->h_iters, p->h_berr, p->d_corder,
-                    p->d_ccounters};
+    void *ptrs[] = {p->d_n,   p->d_order, p->d_counters, p->d_fb_list,  p->d_kind,      p->d_aoff,   p->d_boff,
+                    p->d_work, p->d_work64, p->h_a,      p->h_b,        p->h_x,         p->h_info,   p->h_iters,
+                    p->h_berr, p->d_corder, p->d_ccounters, p->d_gate, p->d_gate_pos, p->d_aoff_h, p->d_boff_h};
     for (void *q : ptrs)
         if (q) cudaFree(q);
+    if (p->h_one) cudaFreeHost(p->h_one);
 }
 
 }  // namespace

@@ -27,8 +27,16 @@ struct BatchDesc {
     double *berr;            // normwise backward error ||b - Ax|| / (||A|| ||x|| + ||b||), inf-norms
     int iters_tag;           // value written to iters by a plain pass (0, or -1 for fallback)
     int max_iters;           // refinement limit (mixed)
-    int warp_small;          // 1: `order` is largest-cost first (n^3, x2 for LU), so the
-                             // small tail may go to the warp-per-system path
+    int warp_small;          // 1: `order` is largest-cost first (n^3, x2 for LU) from position
+                             // warp_from on, so that small tail may go to the warp-per-system path
+    int warp_from;
+    // Host path, one launch for all chunks: chunk c owns the order positions
+    // [gate_pos[c], gate_pos[c + 1]) and its inputs are on the device once gate[c] != 0
+    // (written by the copy stream after the chunk's copies). gate_n = 0: no gating.
+    const int *gate;
+    const int *gate_pos;
+    int gate_n;
+    int *gate_err;           // set when a wait for a chunk ran out (1 s); the CTA then stops
 };
 
 // Systems of cost n^3 (x2 for LU) at most this go one per warp: a Cholesky n <= 32 or an
@@ -154,21 +162,68 @@ __device__ void batch_solve_one(const BatchDesc &d, int sys, const TI *__restric
     __syncthreads();
 }
 
-template <class TI, class TF, bool MIXED>
+// Waits (one thread) until *flag != 0, sleeping between polls, at most 1 s of wall time;
+// false if it ran out. The flag is written by a copy after the chunk's data copies on the
+// same stream, so the data is in device memory once the flag is seen.
+__device__ __forceinline__ bool gate_wait(const int *flag) {
+    unsigned long long t0, t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    for (;;) {
+        int v;
+        asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(flag) : "memory");
+        if (v != 0) return true;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        if (t - t0 > 1000000000ull) return false;
+        __nanosleep(256);
+    }
+}
+
+// The next position of the queue (one thread); with gating, waits until the position's
+// chunk is on the device (gate_ok = 0 if the wait ran out). Out of line: it keeps the
+// gate bookkeeping out of the solver's registers.
+static __device__ __noinline__ int dequeue(const BatchDesc &d, int count, int &gate, int &gate_ok) {
+    const int it = atomicAdd(d.next, 1);
+    gate_ok = 1;
+    if (d.gate_n > 0 && it < count) {
+        int c = 0;
+        while (c + 1 < d.gate_n && it >= d.gate_pos[c + 1]) c++;
+        if (c > gate) {
+            gate_ok = gate_wait(d.gate + c);
+            if (gate_ok)
+                gate = c;  // chunks arrive in order: every chunk up to c is in
+            else
+                atomicExch(d.gate_err, 1);
+        }
+    }
+    return it;
+}
+
+// GATED: the host path's single launch over chunks that are still arriving (dequeue()
+// waits on the chunk flags); a separate instantiation, so the device path's kernel
+// carries none of it.
+template <class TI, class TF, bool MIXED, bool GATED = false>
 __global__ void __launch_bounds__(CTA_THREADS, CtaOcc<TF>::value) batch_solve_kernel(BatchDesc d, const TI *A, const TI *B, TI *X) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CtaSmem<TF> &S = *reinterpret_cast<CtaSmem<TF> *>(smem_raw);
     TF *W = static_cast<TF *>(d.work) + (long long)blockIdx.x * d.work_stride;
     const int count = d.count_dev ? *d.count_dev : d.count;
+    __shared__ int s_gate, s_gate_ok;  // highest chunk seen on the device; this item's chunk arrived
+    if (GATED && threadIdx.x == 0) s_gate = -1;
     for (;;) {
-        if (threadIdx.x == 0) S.item = atomicAdd(d.next, 1);
+        if (threadIdx.x == 0) {
+            if (GATED)
+                S.item = dequeue(d, count, s_gate, s_gate_ok);
+            else
+                S.item = atomicAdd(d.next, 1);
+        }
         __syncthreads();
         const int it = S.item;
+        const bool gate_ok = !GATED || s_gate_ok != 0;
         __syncthreads();
-        if (it >= count) return;
+        if (it >= count || !gate_ok) return;  // done, or a chunk never arrived (gate_err is set)
         const int sys0 = d.order[it], n0 = d.n[sys0];
         const bool small = (double)n0 * n0 * n0 * (d.kind[sys0] ? 1.0 : 2.0) <= kWarpCost;
-        if (small && !d.warp_small) {
+        if (small && (!d.warp_small || (GATED && it < d.warp_from))) {
             // an unordered list (the fallback pass): the small system still takes the
             // warp path, so its arithmetic is the same in every pass
             if (threadIdx.x < 32) warp_solve_small<TI, TF, MIXED>(d, sys0, A, B, X, S.P);
