@@ -489,22 +489,29 @@ static __global__ void __launch_bounds__(256) qr_panel_kernel(T *P, long long ld
 }
 
 // Householder panel on one thread-block cluster (up to 16 CTAs): qr_panel_kernel's
-// algorithm with the two cross-CTA sums per column (sigma, then u = A^T v) read from
-// the other CTAs' shared memory after a cluster barrier. The sums run over the CTAs in
-// rank order in every CTA, so every CTA computes the same tau and u. A column with
-// sigma = 0 still passes a second barrier, so every CTA runs the same barrier sequence,
-// and a last barrier keeps shared memory alive until no other CTA reads it.
+// algorithm with the two cross-CTA sums per column (sigma, then u = A^T v) exchanged on
+// chip. Each CTA pushes its partial sums (and x0, from the CTA holding row j) into every
+// CTA's tables by remote shared-memory stores before a cluster barrier; after it every
+// CTA adds the C partials from its own tables in rank order, so all compute the same tau
+// and u with no remote read on the critical path. v_r = a_rj / v0 is formed once per
+// row (it was formed again for every column of the u sums). The tables are written for
+// column j + 1 only after the barrier that every CTA reaches once it has read them for
+// column j. A column with sigma = 0 still passes the second barrier, so every CTA runs
+// the same barrier sequence.
 template <class T>
 static __global__ void __launch_bounds__(256) qr_panel_cluster_kernel(T *P, long long lda, int mrows, int kb,
                                                               int rows_per, T *tau) {
     namespace cg = cooperative_groups;
     constexpr int NB = PanelNB<T>::value;
     constexpr int LDR = NB + 1;
+    constexpr int CMAX = 16;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *R = reinterpret_cast<T *>(smem_raw);  // rows_per x LDR
-    T *u = R + (size_t)rows_per * LDR;       // NB: this column's u (all CTAs)
-    T *upart = u + NB;                       // NB: this CTA's partial of u
-    T *misc = upart + NB;                    // [0] this CTA's sigma partial, [1] x0 (owner of row j)
+    T *vb = R + (size_t)rows_per * LDR;      // rows_per: this column's v for the owned rows
+    T *u = vb + rows_per;                    // NB: this column's u
+    T *up_tab = u + NB;                      // CMAX x NB: every CTA's partial of u
+    T *sig_tab = up_tab + CMAX * NB;         // CMAX: every CTA's partial of sigma
+    T *x0_slot = sig_tab + CMAX;             // 1: x0 = a_jj from the CTA holding row j
     __shared__ T s_red[8];
     cg::cluster_group cluster = cg::this_cluster();
     const int C = (int)cluster.num_blocks(), g = (int)cluster.block_rank();
@@ -517,8 +524,7 @@ static __global__ void __launch_bounds__(256) qr_panel_cluster_kernel(T *P, long
     }
     __syncthreads();
     for (int j = 0; j < kb; j++) {
-        const int owner_j = j / rows_per;
-        // (1) sigma partial over rows > j
+        // (1) sigma partial over rows > j, pushed (with x0) to every CTA
         T sp = T(0);
         for (int r = max(j + 1 - r0, 0) + tid; r < nr; r += blockDim.x) {
             const T v = R[r * LDR + j];
@@ -527,23 +533,22 @@ static __global__ void __launch_bounds__(256) qr_panel_cluster_kernel(T *P, long
         sp = warp_sum(sp);
         if (lane == 0) s_red[warp] = sp;
         __syncthreads();
-        if (tid == 0) {
+        if (tid < C) {
             T t = T(0);
             for (int w = 0; w < nw; w++) t += s_red[w];
-            misc[0] = t;
-            if (j >= r0 && j < r1) misc[1] = R[(j - r0) * LDR + j];
+            *cluster.map_shared_rank(sig_tab + g, tid) = t;
+            if (j >= r0 && j < r1) *cluster.map_shared_rank(x0_slot, tid) = R[(j - r0) * LDR + j];
         }
         cluster.sync();
-        // sigma over the CTAs in rank order (lane q reads CTA q), x0 from row j's owner
-        T sigma = T(0);
+        // sigma over the CTAs in rank order (lane q holds CTA q's partial)
         if (warp == 0) {
-            sigma = lane < C ? cluster.map_shared_rank(misc, lane)[0] : T(0);
+            T sigma = lane < C ? sig_tab[lane] : T(0);
             sigma = warp_sum(sigma);
             if (lane == 0) s_red[0] = sigma;
         }
         __syncthreads();
-        sigma = s_red[0];
-        const T x0 = cluster.map_shared_rank(misc, owner_j)[1];
+        const T sigma = s_red[0];
+        const T x0 = *x0_slot;
         if (sigma == T(0)) {  // already a multiple of e1: tau = 0, nothing changes
             if (g == 0 && tid == 0) tau[j] = T(0);
             cluster.sync();
@@ -554,29 +559,32 @@ static __global__ void __launch_bounds__(256) qr_panel_cluster_kernel(T *P, long
         const T two = T(2);
         const T t = two * v0 * v0 / (v0 * v0 + sigma);
         if (g == 0 && tid == 0) tau[j] = t;
-        // (2) u_c partial = sum_r v_r a[r][c] for c >= j over owned rows r >= j
+        // v of the owned rows below the diagonal (stored into the panel by the update)
+        for (int r = max(j + 1 - r0, 0) + tid; r < nr; r += blockDim.x) vb[r] = R[r * LDR + j] / v0;
+        __syncthreads();
+        // (2) u_c partial = sum_r v_r a[r][c] for c >= j over owned rows r >= j, pushed
         for (int c = j + warp; c < kb; c += nw) {
             T acc = T(0);
             for (int r = max(j - r0, 0) + lane; r < nr; r += 32) {
-                const T vr = (r0 + r == j) ? T(1) : R[r * LDR + j] / v0;
+                const T vr = (r0 + r == j) ? T(1) : vb[r];
                 acc = fma(vr, R[r * LDR + c], acc);
             }
-            acc = warp_sum(acc);
-            if (lane == 0) upart[c] = acc;
+            acc = __shfl_sync(0xffffffffu, warp_sum(acc), 0);  // lane 0's sum, in every lane
+            if (lane < C) *cluster.map_shared_rank(up_tab + g * NB + c, lane) = acc;
         }
         cluster.sync();
         if (tid >= j && tid < kb) {
             T a = T(0);
-            for (int q = 0; q < C; q++) a += cluster.map_shared_rank(upart, q)[tid];
+            for (int q = 0; q < C; q++) a += up_tab[q * NB + tid];
             u[tid] = a;
         }
         __syncthreads();
         // (3) a[r][c] += (-tau v_r) u_c for c > j; the diagonal becomes x0 - tau u_j and
-        // v[1..] is stored below it
+        // v[1..] stays below it
         for (int r = max(j - r0, 0) + tid; r < nr; r += blockDim.x) {
             T *row = R + r * LDR;
             const bool diag = (r0 + r == j);
-            const T vr = diag ? T(1) : row[j] / v0;
+            const T vr = diag ? T(1) : vb[r];
             const T sc = -t * vr;
             for (int c = j + 1; c < kb; c++) row[c] = fma(sc, u[c], row[c]);
             row[j] = diag ? x0 - t * u[j] : vr;
@@ -587,7 +595,7 @@ static __global__ void __launch_bounds__(256) qr_panel_cluster_kernel(T *P, long
         const int r = idx / kb, c = idx - r * kb;
         P[(long long)(r0 + r) * lda + c] = R[r * LDR + c];
     }
-    cluster.sync();  // no CTA leaves while another may still read its shared memory
+    cluster.sync();  // no CTA leaves while another may still store into its shared memory
 }
 
 // ------------------------------------------------------------------- row swaps --

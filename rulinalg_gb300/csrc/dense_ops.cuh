@@ -157,7 +157,7 @@ rl_status qr_panel_cluster(T *P, long long lda, int mrows, int kb, T *tau, cudaS
     launched = false;
     auto kern = qr_panel_cluster_kernel<T>;
     static const int cmax = probe_cluster(kern, kClusterSmem);
-    const size_t row_bytes = (NB + 1) * sizeof(T), extra = (2 * NB + 2) * sizeof(T);
+    const size_t row_bytes = (NB + 2) * sizeof(T), extra = (NB + 16 * NB + 16 + 1) * sizeof(T);
     int rows_per = 0;
     const int C = cluster_shape(mrows, row_bytes, extra, cmax, panel_target_rows<T>(), rows_per);
     if (C == 0) return RL_OK;
