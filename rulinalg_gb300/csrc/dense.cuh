@@ -246,19 +246,19 @@ __device__ __forceinline__ void warp_amax_key(unsigned long long &k, int &i) {
 // what shortens a column. Per column:
 //   1. each thread searches column j of its rows (the thread that wrote them), the warps
 //      reduce on integer keys, one CTA barrier, every thread combines the warps' maxima;
-//   2. the CTA copies its candidate row (and row j, if it holds it) into a local slot and
-//      pushes its record (key, row, 1 / pivot) into slot g of every CTA's record table
-//      by remote shared-memory stores;
-//   3. one cluster barrier (release / acquire); every warp picks the same winner from its
-//      own CTA's table; threads c < kb read column c of the winning row and of row j
-//      from the CTAs that hold them (one remote round trip); one CTA barrier;
+//   2. the CTA pushes its candidate row (and row j, if it holds it) into every CTA's
+//      tables with 16-byte remote shared-memory stores, and its record (key, row,
+//      1 / pivot);
+//   3. one cluster barrier (release / acquire); every warp picks the same winner from
+//      its own CTA's table, where the winning row and row j already are;
 //   4. the swap and the update run at once, each element stored by one thread: thread
 //      c < kb stores column c of the new row j and, for c < j, of row wi; the threads of
 //      row wi compute its columns >= j from the old row j; every other row below j
 //      updates itself, the multiplier broadcast within the row's threads by a shuffle.
-// Slots and records are double-buffered by column parity: a CTA writes slot s again only
-// after the next cluster barrier, which every CTA reaches after it has read slot s. Every
-// CTA runs the same barrier sequence (a failing pivot is seen by all at the same column).
+// Tables and records are double-buffered by column parity: a CTA writes slot s again
+// only after the next cluster barrier, which every CTA reaches after it has read slot s.
+// Every CTA runs the same barrier sequence (a failing pivot is seen by all at the same
+// column).
 template <class T>
 static __global__ void __launch_bounds__(256) lu_panel_cluster_kernel(T *P, long long lda, int mrows, int kb, int k0,
                                                               int rows_per, int tpr, int *ipiv, int *err, T tiny) {
@@ -266,12 +266,11 @@ static __global__ void __launch_bounds__(256) lu_panel_cluster_kernel(T *P, long
     constexpr int NB = PanelNB<T>::value;
     constexpr int LDR = NB + 1;
     constexpr int CMAX = 16;
+    constexpr int VW = 16 / (int)sizeof(T), NCH = NB / VW;  // 16-byte chunks of a row
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *R = reinterpret_cast<T *>(smem_raw);    // rows_per x LDR
-    T *cand = R + (size_t)rows_per * LDR;      // 2 x NB, this CTA's candidate row per parity
-    T *rowj = cand + 2 * NB;                   // 2 x NB, row j when this CTA holds it
-    T *prow = rowj + 2 * NB;                   // NB, the pivot row (the new row j)
-    T *oldj = prow + NB;                       // NB, the old row j (the new row wi)
+    T *tab = reinterpret_cast<T *>(smem_raw);  // 2 x CMAX x NB: every CTA's candidate row
+    T *rowj = tab + 2 * CMAX * NB;             // 2 x NB: row j (pushed by the CTA holding it)
+    T *R = rowj + 2 * NB;                      // rows_per x LDR
     __shared__ unsigned long long s_k[8], rec_k[2 * CMAX];
     __shared__ int s_i[8], rec_i[2 * CMAX];
     __shared__ T rec_inv[2 * CMAX];
@@ -321,9 +320,29 @@ static __global__ void __launch_bounds__(256) lu_panel_cluster_kernel(T *P, long
                 bi = i2;
             }
         }
-        // 2. local copies of the candidate row and row j; the record to every CTA
-        if (bk != 0ull && tid < kb) cand[slot * NB + tid] = R[(bi - r0) * LDR + tid];
-        if (j >= r0 && j < r1 && tid < kb) rowj[slot * NB + tid] = R[(j - r0) * LDR + tid];
+        // 2. push the candidate row (and row j, from the CTA holding it) into every CTA's
+        // tables in 16-byte stores, and the record
+        const int nch = (kb + VW - 1) / VW;
+        if (bk != 0ull)
+            for (int idx = tid; idx < C * nch; idx += blockDim.x) {
+                const int dst = idx / nch, ch = idx - dst * nch;
+                const T *src = R + (size_t)(bi - r0) * LDR + ch * VW;
+                uint4 v;
+                T *vt = reinterpret_cast<T *>(&v);
+#pragma unroll
+                for (int e = 0; e < VW; e++) vt[e] = src[e];
+                *reinterpret_cast<uint4 *>(cluster.map_shared_rank(tab + (slot * CMAX + g) * NB + ch * VW, dst)) = v;
+            }
+        if (j >= r0 && j < r1)
+            for (int idx = tid; idx < C * nch; idx += blockDim.x) {
+                const int dst = idx / nch, ch = idx - dst * nch;
+                const T *src = R + (size_t)(j - r0) * LDR + ch * VW;
+                uint4 v;
+                T *vt = reinterpret_cast<T *>(&v);
+#pragma unroll
+                for (int e = 0; e < VW; e++) vt[e] = src[e];
+                *reinterpret_cast<uint4 *>(cluster.map_shared_rank(rowj + slot * NB + ch * VW, dst)) = v;
+            }
         if (warp == 0) {
             const T inv = bk != 0ull ? T(1) / R[(bi - r0) * LDR + j] : T(0);
             if (lane < C) {
@@ -348,14 +367,9 @@ static __global__ void __launch_bounds__(256) lu_panel_cluster_kernel(T *P, long
         } else {  // no finite candidate (NaN column): keep the diagonal
             wi = j;
         }
-        const int owner_j = j / rows_per;
-        if (tid < kb) {
-            const T o = cluster.map_shared_rank(rowj + slot * NB, owner_j)[tid];
-            oldj[tid] = o;
-            prow[tid] = wg >= 0 ? cluster.map_shared_rank(cand + slot * NB, wg)[tid] : o;
-        }
+        const T *oldj = rowj + slot * NB;                                // the old row j
+        const T *prow = wg >= 0 ? tab + (slot * CMAX + wg) * NB : oldj;  // the pivot row
         if (g == 0 && tid == 0) ipiv[j] = k0 + wi;
-        __syncthreads();
         const T inv_p = wg >= 0 ? rec_inv[slot * CMAX + wg] : T(1) / oldj[j];
         // 4. swap and update
         if (wi != j && tid < kb) {

@@ -138,7 +138,7 @@ rl_status lu_panel_cluster(T *P, long long lda, int mrows, int kb, int k0, int *
     launched = false;
     auto kern = lu_panel_cluster_kernel<T>;
     static const int cmax = probe_cluster(kern, kClusterSmem);
-    const size_t row_bytes = (NB + 1) * sizeof(T), extra = 6 * NB * sizeof(T);
+    const size_t row_bytes = (NB + 1) * sizeof(T), extra = (2 * 16 * NB + 2 * NB) * sizeof(T);
     int rows_per = 0;
     const int C = cluster_shape(mrows, row_bytes, extra, cmax, panel_target_rows<T>(), rows_per);
     if (C == 0) return RL_OK;
