@@ -266,7 +266,7 @@ static __global__ void __launch_bounds__(256) lu_panel_cluster_kernel(T *P, long
     constexpr int NB = PanelNB<T>::value;
     constexpr int LDR = NB + 1;
     constexpr int CMAX = 16;
-    constexpr int VW = 16 / (int)sizeof(T), NCH = NB / VW;  // 16-byte chunks of a row
+    constexpr int VW = 16 / (int)sizeof(T);  // elements per 16-byte chunk of a row
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *tab = reinterpret_cast<T *>(smem_raw);  // 2 x CMAX x NB: every CTA's candidate row
     T *rowj = tab + 2 * CMAX * NB;             // 2 x NB: row j (pushed by the CTA holding it)
