@@ -1,0 +1,54 @@
+"""Host-side behaviour of the Python mirror of rulinalg's types that needs no GPU: the
+reference's assert!-panics on misuse (raised before any library call, with the
+reference's messages) and `PartialPivLu::unpack` (lu.rs:138-149) on a compact LU from
+the oracle, checked against the reference's exact 3x3 known answer
+(tests/mat/mod.rs:104-125)."""
+import numpy as np
+import pytest
+
+import oracle as O
+from comparators import assert_matrix_float_eq, perm_from_matrix
+
+
+def A(x):
+    return np.array(x, dtype=np.float64)
+
+
+def test_mat_mul_dimension_panic(rl):
+    with pytest.raises(rl.RulinalgPanic, match="Matrix dimensions do not agree"):  # mat_mul.rs:21
+        rl.mat_mul(np.zeros((2, 3)), np.zeros((2, 3)))
+
+
+def test_lu_panics(rl):
+    with pytest.raises(rl.RulinalgPanic, match="square for LU"):  # lu.rs:165
+        rl.PartialPivLu.decompose(np.zeros((3, 4)))
+    lu = rl.PartialPivLu(np.eye(3), np.arange(3, dtype=np.uint64))
+    with pytest.raises(rl.RulinalgPanic, match="compatible size"):  # lu.rs:232
+        lu.solve(np.ones(4))
+
+
+def test_cholesky_panics(rl):
+    with pytest.raises(rl.RulinalgPanic, match="square for Cholesky"):  # cholesky.rs:117
+        rl.Cholesky.decompose(np.zeros((2, 3)))
+    with pytest.raises(rl.RulinalgPanic, match="dimensionally compatible"):  # cholesky.rs:195
+        rl.Cholesky(np.eye(3)).solve(np.ones(2))
+
+
+def test_lstsq_mixed_panics(rl):
+    with pytest.raises(rl.RulinalgPanic):
+        rl.lstsq_mixed(np.zeros(5), np.zeros(5))
+    with pytest.raises(rl.RulinalgPanic):
+        rl.lstsq_mixed(np.zeros((6, 3)), np.zeros(5))
+
+
+def test_lu_unpack_matches_reference_3x3(rl, golden):
+    c = golden["lu_exact_3x3"]
+    lu, perm, st = O.lu_decompose(A(c["a"]))
+    assert st == O.OK
+    lup = rl.PartialPivLu(lu, perm).unpack()
+    assert_matrix_float_eq(lup.l, A(c["l"]))
+    assert_matrix_float_eq(lup.u, A(c["u"]))
+    assert np.array_equal(lup.p.perm, perm_from_matrix(c["p"]))
+    # unit lower / upper structure
+    assert np.array_equal(np.diag(lup.l), np.ones(3)) and not np.triu(lup.l, 1).any()
+    assert not np.tril(lup.u, -1).any()
