@@ -93,10 +93,9 @@ int probe_cluster(K kern, size_t smem) {
 // bytes per CTA: about `target_rows` rows per CTA, clamped to [2, cmax] and to at least
 // the CTAs that the shared memory needs; 0 when even cmax CTAs would need more than
 // kClusterSmem bytes each. FP64 panels take 64 rows per CTA (their row updates run at
-// the SM's FP64 rate, so every SM added shortens a column); FP32 panels take 256, which
-// measured the same alone and keeps clusters small enough to be placed next to the
-// other streams' kernels in the serving loop (16-CTA FP32 clusters halved its
-// throughput: a cluster needs that many SMs of one GPC at once).
+// the SM's FP64 rate, so every SM added shortens a column); FP32 panels take 256 (their
+// updates are cheap: up to 16 CTAs measured the same), which leaves the SMs of a GPC to
+// other streams' kernels where fewer will do.
 template <class T>
 constexpr int panel_target_rows() {
     return sizeof(T) == 8 ? 64 : 256;
@@ -241,8 +240,6 @@ rl_status chol_factor_dev(T *A, long long lda, int n, cudaStream_t s, T tiny = E
     return RL_OK;
 }
 
-// Blocked Householder QR with compact-WY trailing updates; nrefl reflectors
-// (min(m, n) for a plain QR; n for the augmented least-squares matrix).
 // Tm of a reflector block V (mrows x kb): partial Gram matrices, then the T recursion.
 template <class T>
 rl_status block_t_factor(const T *V, int mrows, int kb, const T *tau, T *part, int max_parts, T *Tm,
@@ -256,6 +253,8 @@ rl_status block_t_factor(const T *V, int mrows, int kb, const T *tau, T *part, i
     return RL_OK;
 }
 
+// Blocked Householder QR with compact-WY trailing updates; nrefl reflectors
+// (min(m, n) for a plain QR; n for the augmented least-squares matrix).
 template <class T>
 rl_status qr_factor_dev(T *A, long long lda, int m, int n, int nrefl, T *tau, cudaStream_t s) {
     if (nrefl <= 0) return RL_OK;
