@@ -151,14 +151,33 @@ def run_oracle(idx, n, kind, a_host, b_host, threads):
     return dt, info
 
 
+def workloads_module():
+    """rulinalg_gb300/workloads.py loaded by its path: the package's __init__ loads the
+    CUDA library, which the reference arm must not map (it is numpy-only)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("rl_bench_workloads", ROOT / "rulinalg_gb300" / "workloads.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def batch_config(args, world, n):
+    """The `config` of the headline line, identical in both arms."""
+    a_gb = float(np.sum(np.asarray(n, dtype=np.float64) ** 2)) * 8 / 1e9
+    return {"workload": "batched uneven solves: 20k SPD (Cholesky) + 20k general (PartialPivLu)",
+            "count_spd": args.count_spd, "count_lu": args.count_lu, "n_range": [8, 512], "rhs": 1,
+            "seed": args.seed, "parallelism": f"replicas x{world}",
+            "l2": f"inputs {a_gb:.1f} GB of f64 matrices > 129 MB L2, no flush needed"}
+
+
 def reference_arm(args, rank, world):
-    """The reference's algorithms (oracle restatement) on all host threads."""
+    """The reference's algorithms (the oracle's C restatement of PartialPivLu / Cholesky
+    decompose + solve) on all host threads, on a seeded quarter of the batch's work."""
     if rank != 0:
         return
-    from rulinalg_gb300.workloads import mixed_batch
-    n, kind, a, b = mixed_batch(args.count_spd, args.count_lu, seed=args.seed)
+    n, kind, a, b = workloads_module().mixed_batch(args.count_spd, args.count_lu, seed=args.seed)
     threads = os.cpu_count() or 1
-    idx = cpu_sample(n, kind, args.cpu_sample_gflop * threads / 4, args.seed)
+    idx = cpu_sample(n, kind, flops_of(n, kind) / 4e9, args.seed)
     for _ in range(max(0, args.warmup)):
         run_oracle(idx[: max(1, len(idx) // 8)], n, kind, a, b, threads)
     times = []
@@ -166,16 +185,19 @@ def reference_arm(args, rank, world):
         dt, info = run_oracle(idx, n, kind, a, b, threads)
         times.append(dt)
     v = len(idx) / statistics.mean(times)
-    sample = f"{len(idx)} of {len(n)} systems (seeded sample, {flops_of(n[idx], kind[idx]) / 1e9:.1f} GFLOP of factorisation)"
+    sample = (f"each step: {len(idx)} of {len(n)} systems, a seeded sample carrying a quarter of the batch's "
+              f"factorisation work ({flops_of(n[idx], kind[idx]) / 1e9:.1f} of {flops_of(n, kind) / 1e9:.1f} GFLOP); "
+              f"{threads} POSIX threads taking systems from a shared counter (the reference crate itself is "
+              f"single-threaded); rulinalg-algorithm restatement in C (oracle/), -O2 -ffp-contract=off")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "batched uneven solves (20k SPD + 20k general)", "count_spd": args.count_spd,
-                   "count_lu": args.count_lu, "n_range": [8, 512], "seed": args.seed},
+        "config": batch_config(args, world, n),
         "cpu_baseline": {"value": v, "unit": "solves/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "rulinalg is Rust with no toolchain on this machine; its algorithms run as the C restatement in oracle/",
+        "note": "rulinalg is Rust with no toolchain on this machine; its algorithms run as the C restatement in "
+                "oracle/ (no CUDA library is loaded by this arm)",
     }), flush=True)
 
 
@@ -584,10 +606,7 @@ def main():
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 factor + f64 refinement", "data": "synthetic",
-        "config": {"workload": "batched uneven solves: 20k SPD (Cholesky) + 20k general (PartialPivLu)",
-                   "count_spd": args.count_spd, "count_lu": args.count_lu, "n_range": [8, 512], "rhs": 1,
-                   "seed": args.seed, "parallelism": f"replicas x{world}",
-                   "l2": f"inputs {a_bytes / 1e9:.1f} GB > 129 MB L2, no flush needed"},
+        "config": batch_config(args, world, n),
         "plain_fp64_gpu": {"value": v_fp64, "unit": "solves/s", "ms_per_step": ms_fp64,
                            "speedup_mixed_over_fp64": value / v_fp64},
         "batch_latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))]},

@@ -61,6 +61,29 @@ RL_API rl_status rl_device_check(void);
 /* Number of kernel launches this library has issued in this process (all threads). */
 RL_API uint64_t rl_launch_count(void);
 
+/* -------------------------------------------------------------------- tunables -- */
+/* Process-wide settings of the library (no counterpart in the reference, which has no
+ * launch shapes or device waits). rl_tune_set stores a value for the calls that start
+ * after it (a batched plan takes its launch shape and upload chunks when it is created,
+ * and its wait limit when its launch sequence is recorded); rl_tune_get reads it back.
+ * The batched autotuner (rulinalg_gb300/autotune.py) writes the RL_TUNE_BATCH_* and
+ * RL_TUNE_UPLOAD_CHUNKS values it selects. Out-of-range values return
+ * RL_ERR_INVALID_ARG and change nothing. */
+#define RL_TUNE_WAIT_TIMEOUT_NS 1     /* limit of every device-side wait, ns: [1e6, 1e10], default 1e9 */
+#define RL_TUNE_PANEL_CLUSTER_MAX 2   /* largest thread-block cluster of the blocked LU / QR panels: [0, 16],
+                                         default 16 (capped by the device); 0: always the cooperative grid */
+#define RL_TUNE_BATCH_CTAS_PER_SM 3   /* CTAs per SM of the batched launch: [0, 8], 0 (default): the
+                                         kernel's occupancy; larger values are capped by it */
+#define RL_TUNE_BATCH_WARP_COST 4     /* systems of cost n^3 (x2 for LU) up to this take the one-warp path in
+                                         a largest-first batch: [0, 32768], default 32768 */
+#define RL_TUNE_UPLOAD_CHUNKS 5       /* chunks of the host path's overlapped upload: [1, 256], default 32 */
+#define RL_TUNE_TEST_WITHHOLD_CHUNK 100 /* tests only: the host batched path never sets this chunk's arrival
+                                           flag, so its wait runs out (RL_ERR_TIMEOUT): [-1, 255], default -1 */
+#define RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK 101 /* tests only: the few-right-hand-side triangular sweep never
+                                                 publishes this 64-row block: [-1, 2^30], default -1 */
+RL_API rl_status rl_tune_set(int key, int64_t value);
+RL_API rl_status rl_tune_get(int key, int64_t *value);
+
 /* ------------------------------------------------------------------------ GEMM -- */
 /* C = A * B with A m x k, B k x n, C m x n; alpha = 1, beta = 0.
  * Replaces the matrixmultiply::{sgemm,dgemm} calls of mat_mul_general!

@@ -55,6 +55,9 @@ for sfx, ct in (("d", C.c_double), ("s", C.c_float)):
         ("or_qr_first_k_columns", None, [_sz, _sz, _vp, _sz, _vp, _sz, _vp, _sz]),
         ("or_qr_q_left_multiply", None, [_sz, _sz, _vp, _sz, _vp, _sz, _vp, _sz]),
         ("or_qr_lstsq", C.c_int, [_sz, _sz, _vp, _sz, _vp, _vp]),
+        ("or_gemm_mt", None, [_sz, _sz, _sz, _vp, _sz, _vp, _sz, _vp, _sz, C.c_int]),
+        ("or_lu_decompose_mt", C.c_int, [_sz, _vp, _sz, _vp, _vp, C.c_int]),
+        ("or_solve_columns_mt", C.c_int, [_sz, _vp, _sz, _vp, _sz, _vp, _sz, C.c_int]),
     ):
         f = getattr(_lib, f"{name}_{sfx}")
         f.restype = res
@@ -89,13 +92,17 @@ def dot(u, v):
     return _f(u, "or_dot")(min(len(u), len(v)), _p(u), _p(v))
 
 
-def gemm(a, b):
+def gemm(a, b, threads=1):
+    """The i-k-j GEMM; threads > 1 splits the rows of C (bit-identical results)."""
     a = _m(a)
     b = _m(b, a.dtype)
     m, k = a.shape
     n = b.shape[1]
     c = np.zeros((m, n), dtype=a.dtype)
-    _f(a, "or_gemm")(m, k, n, _p(a), max(k, 1), _p(b), max(n, 1), _p(c), max(n, 1))
+    if threads > 1:
+        _f(a, "or_gemm_mt")(m, k, n, _p(a), max(k, 1), _p(b), max(n, 1), _p(c), max(n, 1), threads)
+    else:
+        _f(a, "or_gemm")(m, k, n, _p(a), max(k, 1), _p(b), max(n, 1), _p(c), max(n, 1))
     return c
 
 
@@ -112,13 +119,17 @@ def norm_frobenius(a):
     return _f(a, "or_norm_frobenius")(a.shape[0], a.shape[1], _p(a), max(a.shape[1], 1))
 
 
-def lu_decompose(a, gaps=False):
-    """Returns (lu, perm, status[, gap per step])."""
+def lu_decompose(a, gaps=False, threads=1):
+    """Returns (lu, perm, status[, gap per step]); threads > 1 splits every step's
+    elimination rows over threads (bit-identical results)."""
     lu = _m(a)
     n = lu.shape[0]
     perm = np.zeros(max(n, 1), dtype=np.uint64)
     gap = np.zeros(max(n, 1), dtype=lu.dtype)
-    st = _f(lu, "or_lu_decompose")(n, _p(lu), max(n, 1), _p(perm), _p(gap) if gaps else None)
+    if threads > 1:
+        st = _f(lu, "or_lu_decompose_mt")(n, _p(lu), max(n, 1), _p(perm), _p(gap) if gaps else None, threads)
+    else:
+        st = _f(lu, "or_lu_decompose")(n, _p(lu), max(n, 1), _p(perm), _p(gap) if gaps else None)
     if gaps:
         return lu, perm[:n], st, gap[:n]
     return lu, perm[:n], st
@@ -129,6 +140,18 @@ def lu_solve(lu, perm, b):
     perm = _m(perm, np.uint64)
     x = _m(b, lu.dtype)
     st = _f(lu, "or_lu_solve")(lu.shape[0], _p(lu), max(lu.shape[0], 1), _p(perm), _p(x))
+    return x, st
+
+
+def solve_columns(lu, perm, b, threads=1):
+    """PartialPivLu::solve (perm given) or Cholesky::solve (perm None) of every column of
+    the n x nrhs array b, columns split over threads. Returns (x, status)."""
+    lu = _m(lu)
+    n = lu.shape[0]
+    x = _m(np.asarray(b).reshape(n, -1), lu.dtype)
+    pp = _m(perm, np.uint64) if perm is not None else None
+    st = _f(lu, "or_solve_columns_mt")(n, _p(lu), max(n, 1), _p(pp) if pp is not None else None, x.shape[1], _p(x),
+                                       max(x.shape[1], 1), threads)
     return x, st
 
 

@@ -427,6 +427,183 @@ int FN(or_qr_lstsq)(size_t m, size_t n, T *a, size_t lda, const T *b, T *x) {
     return st;
 }
 
+/* ------------------------------------------------- threaded variants (tests) -- */
+/* For the configurations' full sizes (n = 1024 .. 4096) the tests split the work of the
+ * functions above over POSIX threads. Each element of the result sees exactly the
+ * operations of the single-threaded function, in the same order (the threads only
+ * partition rows, or right-hand-side columns), so the results are bit-identical to it. */
+
+typedef struct {
+    size_t p, q, r, lda, ldb, ldc, lo, hi;
+    const T *a, *b;
+    T *c;
+} FN(or_gemm_job);
+
+static void *FN(or_gemm_worker)(void *arg) {
+    FN(or_gemm_job) *j = (FN(or_gemm_job) *)arg;
+    FN(or_gemm)(j->hi - j->lo, j->q, j->r, j->a + j->lo * j->lda, j->lda, j->b, j->ldb, j->c + j->lo * j->ldc,
+                j->ldc);
+    return NULL;
+}
+
+/* or_gemm with the rows of C split over `threads` threads (i-k-j per row as there). */
+void FN(or_gemm_mt)(size_t p, size_t q, size_t r, const T *a, size_t lda, const T *b, size_t ldb, T *c, size_t ldc,
+                    int threads) {
+    if (threads < 1) threads = 1;
+    if (threads > 256) threads = 256;
+    if ((size_t)threads > p) threads = p ? (int)p : 1;
+    pthread_t th[256];
+    FN(or_gemm_job) jobs[256];
+    for (int t = 0; t < threads; t++) {
+        FN(or_gemm_job) j = {p, q, r, lda, ldb, ldc, p * (size_t)t / (size_t)threads,
+                             p * (size_t)(t + 1) / (size_t)threads, a, b, c};
+        jobs[t] = j;
+    }
+    for (int t = 1; t < threads; t++) pthread_create(&th[t], NULL, FN(or_gemm_worker), &jobs[t]);
+    FN(or_gemm_worker)(&jobs[0]);
+    for (int t = 1; t < threads; t++) pthread_join(th[t], NULL);
+}
+
+typedef struct {
+    size_t n, lda;
+    T *a;
+    uint64_t *p;
+    T *gap;
+    int tid, threads, status;
+    volatile int *stop;
+    pthread_barrier_t *bar;
+} FN(or_lu_job);
+
+/* One thread of or_lu_decompose_mt: thread 0 runs the pivot search, the failure check
+ * and the row swap of each step (lu.rs:169-190) exactly as or_lu_decompose does; after a
+ * barrier every thread eliminates its contiguous share of the rows below the pivot with
+ * gaussian_elimination's operations (lu.rs:603-616); a second barrier ends the step. */
+static void *FN(or_lu_worker)(void *arg) {
+    FN(or_lu_job) *j = (FN(or_lu_job) *)arg;
+    const size_t n = j->n, lda = j->lda;
+    T *a = j->a;
+    for (size_t index = 0; index < n; index++) {
+        if (j->tid == 0) {
+            size_t curr_max_idx = index;
+            T curr_max = a[index * lda + index];
+            for (size_t i = index + 1; i < n; i++) {
+                if (ABS(a[i * lda + index]) > ABS(curr_max)) {
+                    curr_max = a[i * lda + index];
+                    curr_max_idx = i;
+                }
+            }
+            if (j->gap) {
+                T second = 0;
+                for (size_t i = index; i < n; i++)
+                    if (i != curr_max_idx && ABS(a[i * lda + index]) > second) second = ABS(a[i * lda + index]);
+                j->gap[index] = ABS(curr_max) > 0 ? (ABS(curr_max) - second) / ABS(curr_max) : 0;
+            }
+            if (ABS(curr_max) < EPS) {
+                *j->stop = 1;
+                j->status = RL_ERR_DIV_BY_ZERO;
+            } else if (curr_max_idx != index) {
+                for (size_t c = 0; c < n; c++) {
+                    T t = a[index * lda + c];
+                    a[index * lda + c] = a[curr_max_idx * lda + c];
+                    a[curr_max_idx * lda + c] = t;
+                }
+                uint64_t t = j->p[index];
+                j->p[index] = j->p[curr_max_idx];
+                j->p[curr_max_idx] = t;
+            }
+        }
+        pthread_barrier_wait(j->bar);
+        if (*j->stop) break;
+        const size_t rows = n - index - 1;
+        const size_t lo = index + 1 + rows * (size_t)j->tid / (size_t)j->threads;
+        const size_t hi = index + 1 + rows * (size_t)(j->tid + 1) / (size_t)j->threads;
+        const T piv_val = a[index * lda + index];
+        for (size_t i = lo; i < hi; i++) {
+            const T mult = a[i * lda + index] / piv_val;
+            a[i * lda + index] = mult;
+            for (size_t c = index + 1; c < n; c++) a[i * lda + c] = a[i * lda + c] - mult * a[index * lda + c];
+        }
+        pthread_barrier_wait(j->bar);
+    }
+    return NULL;
+}
+
+/* or_lu_decompose with the elimination rows of every step split over `threads`
+ * threads; bit-identical to it (same pivots, same factors, same status). */
+int FN(or_lu_decompose_mt)(size_t n, T *a, size_t lda, uint64_t *perm_out, T *gap_out, int threads) {
+    if (threads < 1) threads = 1;
+    if (threads > 256) threads = 256;
+    if (threads == 1 || n < 64) return FN(or_lu_decompose)(n, a, lda, perm_out, gap_out);
+    uint64_t *p = (uint64_t *)malloc(((n) + 1) * sizeof(uint64_t));
+    for (size_t i = 0; i < n; i++) p[i] = i;
+    pthread_t th[256];
+    FN(or_lu_job) jobs[256];
+    pthread_barrier_t bar;
+    volatile int stop = 0;
+    pthread_barrier_init(&bar, NULL, (unsigned)threads);
+    for (int t = 0; t < threads; t++) {
+        FN(or_lu_job) j = {n, lda, a, p, gap_out, t, threads, RL_OK, &stop, &bar};
+        jobs[t] = j;
+    }
+    for (int t = 1; t < threads; t++) pthread_create(&th[t], NULL, FN(or_lu_worker), &jobs[t]);
+    FN(or_lu_worker)(&jobs[0]);
+    for (int t = 1; t < threads; t++) pthread_join(th[t], NULL);
+    pthread_barrier_destroy(&bar);
+    const int st = jobs[0].status;
+    if (st == RL_OK && perm_out)
+        for (size_t i = 0; i < n; i++) perm_out[p[i]] = i;
+    free(p);
+    return st;
+}
+
+typedef struct {
+    size_t n, lda, nrhs, ldb, lo, hi;
+    const T *lu;
+    const uint64_t *perm;
+    T *b;
+    int status;
+} FN(or_solve_job);
+
+static void *FN(or_lu_solve_worker)(void *arg) {
+    FN(or_solve_job) *j = (FN(or_solve_job) *)arg;
+    T *col = (T *)malloc(((j->n) + 1) * sizeof(T));
+    j->status = RL_OK;
+    for (size_t c = j->lo; c < j->hi; c++) {
+        for (size_t i = 0; i < j->n; i++) col[i] = j->b[i * j->ldb + c];
+        const int st = j->perm ? FN(or_lu_solve)(j->n, j->lu, j->lda, j->perm, col)
+                               : FN(or_chol_solve)(j->n, j->lu, j->lda, col);
+        if (st != RL_OK) {
+            j->status = st;
+            break;
+        }
+        for (size_t i = 0; i < j->n; i++) j->b[i * j->ldb + c] = col[i];
+    }
+    free(col);
+    return NULL;
+}
+
+/* PartialPivLu::solve (perm != NULL) or Cholesky::solve (perm == NULL) applied to each
+ * column of the n x nrhs row-major B (overwritten by X), columns split over threads. */
+int FN(or_solve_columns_mt)(size_t n, const T *lu, size_t lda, const uint64_t *perm, size_t nrhs, T *b, size_t ldb,
+                            int threads) {
+    if (threads < 1) threads = 1;
+    if (threads > 256) threads = 256;
+    if ((size_t)threads > nrhs) threads = nrhs ? (int)nrhs : 1;
+    pthread_t th[256];
+    FN(or_solve_job) jobs[256];
+    for (int t = 0; t < threads; t++) {
+        FN(or_solve_job) j = {n, lda, nrhs, ldb, nrhs * (size_t)t / (size_t)threads,
+                              nrhs * (size_t)(t + 1) / (size_t)threads, lu, perm, b, RL_OK};
+        jobs[t] = j;
+    }
+    for (int t = 1; t < threads; t++) pthread_create(&th[t], NULL, FN(or_lu_solve_worker), &jobs[t]);
+    FN(or_lu_solve_worker)(&jobs[0]);
+    for (int t = 1; t < threads; t++) pthread_join(th[t], NULL);
+    for (int t = 0; t < threads; t++)
+        if (jobs[t].status != RL_OK) return jobs[t].status;
+    return RL_OK;
+}
+
 #undef FN
 #undef CAT
 #undef CAT2

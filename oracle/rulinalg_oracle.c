@@ -11,8 +11,11 @@
  *
  * Build: see oracle/Makefile (-O2 -ffp-contract=off, no fast-math).
  */
+#define _POSIX_C_SOURCE 200809L
 #include <math.h>
 #include <float.h>
+#include <pthread.h>
+#include <stdatomic.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -85,10 +88,10 @@ int or_perm_validate(size_t n, const uint64_t *perm) {
  * routine; a caller loops). kind[i] = 0: PartialPivLu decompose + solve; 1: Cholesky.
  * a and b are packed, a_off/b_off give each system's start. a is consumed. info[i]
  * receives the status. nthreads > 1 splits the systems over POSIX threads. */
-#include <pthread.h>
 
 typedef struct {
     size_t lo, hi;
+    _Atomic size_t *next; /* shared work counter: systems are taken one at a time */
     const int32_t *n;
     const uint8_t *kind;
     const int64_t *a_off, *b_off;
@@ -100,7 +103,9 @@ static void *or_batch_worker(void *arg) {
     or_batch_job *j = (or_batch_job *)arg;
     uint64_t *perm = NULL;
     size_t cap = 0;
-    for (size_t i = j->lo; i < j->hi; i++) {
+    for (;;) {
+        const size_t i = atomic_fetch_add(j->next, 1);
+        if (i >= j->hi) break;
         size_t n = (size_t)j->n[i];
         double *a = j->a + j->a_off[i];
         double *b = j->b + j->b_off[i];
@@ -129,11 +134,11 @@ void or_batch_solve_d(size_t count, const int32_t *n, const uint8_t *kind, const
     if (nthreads > 256) nthreads = 256;
     pthread_t th[256];
     or_batch_job jobs[256];
-    /* interleaved split by cost would be better balanced; contiguous chunks of the
-       (shuffled) input are close enough for a baseline */
+    _Atomic size_t next = 0; /* the threads take systems one at a time from a shared counter */
     for (int t = 0; t < nthreads; t++) {
-        jobs[t].lo = count * (size_t)t / (size_t)nthreads;
-        jobs[t].hi = count * (size_t)(t + 1) / (size_t)nthreads;
+        jobs[t].lo = 0;
+        jobs[t].hi = count;
+        jobs[t].next = &next;
         jobs[t].n = n;
         jobs[t].kind = kind;
         jobs[t].a_off = a_off;

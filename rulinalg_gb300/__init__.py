@@ -16,3 +16,19 @@ def device_available() -> bool:
 
 def launch_count() -> int:
     return int(lib.rl_launch_count())
+
+
+def tune_set(key: int, value: int) -> None:
+    """Sets a process-wide tunable (rl_tune_set; keys TUNE_* in rulinalg_gb300._lib)."""
+    st = lib.rl_tune_set(key, value)
+    if st != 0:
+        raise ValueError(f"rl_tune_set({key}, {value}): {lib.rl_status_string(st).decode()}")
+
+
+def tune_get(key: int) -> int:
+    import ctypes as C
+    v = C.c_int64(0)
+    st = lib.rl_tune_get(key, C.byref(v))
+    if st != 0:
+        raise ValueError(f"rl_tune_get({key}): {lib.rl_status_string(st).decode()}")
+    return int(v.value)

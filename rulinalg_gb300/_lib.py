@@ -37,6 +37,8 @@ SIGNATURES = {
     "rl_version": (C.c_int, []),
     "rl_device_check": (st, []),
     "rl_launch_count": (C.c_uint64, []),
+    "rl_tune_set": (st, [C.c_int, C.c_int64]),
+    "rl_tune_get": (st, [C.c_int, i64p]),
     "rl_sgemm": (st, [sz, sz, sz, f32p, sz, f32p, sz, f32p, sz]),
     "rl_dgemm": (st, [sz, sz, sz, f64p, sz, f64p, sz, f64p, sz]),
     "rl_sgemm_dev": (st, [sz, sz, sz, vp, sz, vp, sz, vp, sz, vp]),
@@ -122,6 +124,15 @@ class SolveInfo(C.Structure):
     """rl_solve_info"""
     _fields_ = [("iters", C.c_int32), ("gmres_iters", C.c_int32), ("path", C.c_int32), ("reserved", C.c_int32),
                 ("berr", C.c_double)]
+
+# RL_TUNE_* keys (rulinalg_gb300.h)
+TUNE_WAIT_TIMEOUT_NS = 1
+TUNE_PANEL_CLUSTER_MAX = 2
+TUNE_BATCH_CTAS_PER_SM = 3
+TUNE_BATCH_WARP_COST = 4
+TUNE_UPLOAD_CHUNKS = 5
+TUNE_TEST_WITHHOLD_CHUNK = 100
+TUNE_TEST_WITHHOLD_SWEEP_BLOCK = 101
 
 for _name, (_res, _args) in SIGNATURES.items():
     _fn = getattr(lib, _name)

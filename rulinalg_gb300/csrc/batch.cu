@@ -63,6 +63,8 @@ rl_status occupancy_grid(size_t smem, int &grid) {
     int per_sm = 0;
     RL_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, CTA_THREADS, smem));
     if (per_sm < 1) return RL_ERR_CUDA;
+    const int64_t want = tune(RL_TUNE_BATCH_CTAS_PER_SM);  // 0: as many as fit
+    if (want > 0 && want < per_sm) per_sm = (int)want;
     grid = per_sm * num_sms();
     return RL_OK;
 }
@@ -90,6 +92,8 @@ rl_status record(rl_batch_plan *p, const TI *a, const TI *b, TI *x, int *info, i
     d.iters_tag = 0;
     d.max_iters = 30;
     d.warp_small = 1;  // the order is largest-cost first
+    d.warp_cost = (int)tune(RL_TUNE_BATCH_WARP_COST);
+    d.wait_ns = wait_ns();
     RL_LAUNCH((batch_solve_kernel<TI, TF, MIXED>), p->grid, CTA_THREADS, p->smem, s, d, a, b, x);
     if (MIXED) {
         BatchDesc f = d;
@@ -167,6 +171,8 @@ rl_status launch_gated(rl_batch_plan *p, const TI *a, const TI *b, TI *x, cudaSt
     d.gate_pos = p->d_gate_pos;
     d.gate_n = (int)p->chunk_first.size();
     d.gate_err = ctr + 3;
+    d.wait_ns = wait_ns();
+    d.warp_cost = (int)tune(RL_TUNE_BATCH_WARP_COST);
     static const cudaError_t attr = cudaFuncSetAttribute(batch_solve_kernel<TI, TF, MIXED, true>,
                                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem);
     RL_TRY_CUDA(attr);
@@ -216,6 +222,7 @@ rl_status solve_host(rl_batch_plan *p, const TI *a, const TI *b, TI *x, int32_t 
     RL_TRY_CUDA(cudaMemsetAsync(p->d_gate, 0, nch * sizeof(int), s));
     RL_TRY_CUDA(cudaEventRecord(p->ev_start, s));  // earlier work on the buffers, and the resets, first
     RL_TRY_CUDA(cudaStreamWaitEvent(p->copy, p->ev_start, 0));
+    const int withhold = (int)tune(RL_TUNE_TEST_WITHHOLD_CHUNK);  // tests: a flag nothing sets
     for (int c = 0; c < nch; c++) {
         const int first = p->chunk_first[c], end = first + p->chunk_count[c];
         const long long a0 = p->a_off[first], a1 = end < (int)p->count ? p->a_off[end] : p->a_total;
@@ -226,7 +233,8 @@ rl_status solve_host(rl_batch_plan *p, const TI *a, const TI *b, TI *x, int32_t 
         if (b1 > b0)
             RL_TRY_CUDA(cudaMemcpyAsync(db + b0 + p->b_shift[c], b + b0, (b1 - b0) * sizeof(TI), cudaMemcpyHostToDevice,
                                         p->copy));
-        RL_TRY_CUDA(cudaMemcpyAsync(p->d_gate + c, p->h_one, sizeof(int), cudaMemcpyHostToDevice, p->copy));
+        if (c != withhold)
+            RL_TRY_CUDA(cudaMemcpyAsync(p->d_gate + c, p->h_one, sizeof(int), cudaMemcpyHostToDevice, p->copy));
     }
     rl_status st;
     if (std::is_same<TI, float>::value)
@@ -294,12 +302,13 @@ rl_status plan_init(rl_batch_plan *p, size_t count, const int32_t *n, const uint
     RL_TRY(upload(p->d_aoff, p->a_off, s));
     RL_TRY(upload(p->d_boff, p->b_off, s));
     RL_TRY(upload(p->d_order, order, s));
-    // Host-path chunks: up to 32 contiguous ranges of about equal matrix bytes, each with
+    // Host-path chunks: up to RL_TUNE_UPLOAD_CHUNKS (32 by default) contiguous ranges of
+    // about equal matrix bytes, each with
     // its own largest-first order. Small chunks shorten both ends of the pipeline (the
     // solve starts after the first chunk's copy and ends a chunk's solve after the last
     // one's); with one gated launch there is no drain between chunks to pay for them.
     {
-        const int want = (int)std::min<size_t>(32, std::max<size_t>(1, count));
+        const int want = (int)std::min<size_t>((size_t)tune(RL_TUNE_UPLOAD_CHUNKS), std::max<size_t>(1, count));
         std::vector<int> corder;
         corder.reserve(count);
         size_t i = 0;

@@ -36,7 +36,9 @@ struct BatchDesc {
     const int *gate;
     const int *gate_pos;
     int gate_n;
-    int *gate_err;           // set when a wait for a chunk ran out (1 s); the CTA then stops
+    int *gate_err;           // set when a wait for a chunk ran out; the CTA then stops
+    unsigned long long wait_ns;  // limit of a chunk wait (RL_TUNE_WAIT_TIMEOUT_NS)
+    int warp_cost;           // systems of cost n^3 (x2 for LU) up to this go one per warp (<= kWarpCost)
 };
 
 // Systems of cost n^3 (x2 for LU) at most this go one per warp: a Cholesky n <= 32 or an
@@ -162,10 +164,10 @@ __device__ void batch_solve_one(const BatchDesc &d, int sys, const TI *__restric
     __syncthreads();
 }
 
-// Waits (one thread) until *flag != 0, sleeping between polls, at most 1 s of wall time;
-// false if it ran out. The flag is written by a copy after the chunk's data copies on the
-// same stream, so the data is in device memory once the flag is seen.
-__device__ __forceinline__ bool gate_wait(const int *flag) {
+// Waits (one thread) until *flag != 0, sleeping between polls, at most `limit` ns of wall
+// time; false if it ran out. The flag is written by a copy after the chunk's data copies
+// on the same stream, so the data is in device memory once the flag is seen.
+__device__ __forceinline__ bool gate_wait(const int *flag, unsigned long long limit) {
     unsigned long long t0, t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
     for (;;) {
@@ -173,7 +175,7 @@ __device__ __forceinline__ bool gate_wait(const int *flag) {
         asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(flag) : "memory");
         if (v != 0) return true;
         asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-        if (t - t0 > 1000000000ull) return false;
+        if (t - t0 > limit) return false;
         __nanosleep(256);
     }
 }
@@ -188,7 +190,7 @@ static __device__ __noinline__ int dequeue(const BatchDesc &d, int count, int &g
         int c = 0;
         while (c + 1 < d.gate_n && it >= d.gate_pos[c + 1]) c++;
         if (c > gate) {
-            gate_ok = gate_wait(d.gate + c);
+            gate_ok = gate_wait(d.gate + c, d.wait_ns);
             if (gate_ok)
                 gate = c;  // chunks arrive in order: every chunk up to c is in
             else
@@ -222,7 +224,7 @@ __global__ void __launch_bounds__(CTA_THREADS, CtaOcc<TF>::value) batch_solve_ke
         __syncthreads();
         if (it >= count || !gate_ok) return;  // done, or a chunk never arrived (gate_err is set)
         const int sys0 = d.order[it], n0 = d.n[sys0];
-        const bool small = (double)n0 * n0 * n0 * (d.kind[sys0] ? 1.0 : 2.0) <= kWarpCost;
+        const bool small = (double)n0 * n0 * n0 * (d.kind[sys0] ? 1.0 : 2.0) <= (double)d.warp_cost;
         if (small && (!d.warp_small || (GATED && it < d.warp_from))) {
             // an unordered list (the fallback pass): the small system still takes the
             // warp path, so its arithmetic is the same in every pass

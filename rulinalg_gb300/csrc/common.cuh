@@ -107,6 +107,10 @@ inline int ceil_div(long long a, long long b) { return static_cast<int>((a + b -
 
 int num_sms();
 
+// The current value of a process-wide tunable (RL_TUNE_* in rulinalg_gb300.h).
+int64_t tune(int key);
+inline unsigned long long wait_ns() { return (unsigned long long)tune(RL_TUNE_WAIT_TIMEOUT_NS); }
+
 // Set on threads that share the GPU with other streams of this library (the serving
 // loop's workers): kernels whose CTAs wait on other CTAs of the same launch, holding
 // their SMs meanwhile, are replaced there by chains of short launches. Measured on the

@@ -20,9 +20,8 @@ struct PanelNB {
 
 // ------------------------------------------------------------------ grid barrier --
 // All CTAs of a cooperative launch arrive on `ctr`; thread 0 spins (bounded by
-// kBarrierTimeoutNs of wall time) until the count reaches `target`. On timeout the
-// error word is set and every CTA leaves the kernel at its next barrier.
-constexpr unsigned long long kBarrierTimeoutNs = 1000000000ull;  // 1 s
+// `limit` ns of wall time, RL_TUNE_WAIT_TIMEOUT_NS) until the count reaches `target`.
+// On timeout the error word is set and every CTA leaves the kernel at its next barrier.
 
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;
@@ -40,7 +39,7 @@ __device__ __forceinline__ void st_release(int *p, int v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-static __device__ bool grid_barrier(unsigned *ctr, unsigned target, int *err) {
+static __device__ bool grid_barrier(unsigned *ctr, unsigned target, int *err, unsigned long long limit) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -54,7 +53,7 @@ static __device__ bool grid_barrier(unsigned *ctr, unsigned target, int *err) {
                 ok = 0;
                 break;
             }
-            if (global_ns() - t0 > kBarrierTimeoutNs) {
+            if (global_ns() - t0 > limit) {
                 atomicCAS(err, 0, RL_ERR_TIMEOUT);
                 ok = 0;
                 break;
@@ -84,7 +83,8 @@ struct PanelSync {
 // cand: 2 slots x G x (2 + NB) values, rowj: 2 slots x NB values.
 template <class T>
 static __global__ void __launch_bounds__(256) lu_panel_kernel(T *P, long long lda, int mrows, int kb, int k0, int rows_per,
-                                                       int *ipiv, T *cand, T *rowj, PanelSync *sync, T tiny) {
+                                                       int *ipiv, T *cand, T *rowj, PanelSync *sync, T tiny,
+                                                       unsigned long long wait_ns) {
     constexpr int NB = PanelNB<T>::value;
     constexpr int LDR = NB + 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -133,7 +133,7 @@ static __global__ void __launch_bounds__(256) lu_panel_kernel(T *P, long long ld
         }
         if (bi != INT_MAX && tid < kb) mine[2 + tid] = R[(bi - r0) * LDR + tid];
         if (j >= r0 && j < r1 && tid < kb) rowj[slot * NB + tid] = R[(j - r0) * LDR + tid];
-        if (!grid_barrier(&sync->ctr, (unsigned)(G * (j + 1)), &sync->err)) return;
+        if (!grid_barrier(&sync->ctr, (unsigned)(G * (j + 1)), &sync->err, wait_ns)) return;
         // Winner over all CTAs, identical in every CTA: thread q reads CTA q's candidate,
         // then a block argmax (largest |v|, smallest row on ties).
         T wv = T(-1);
@@ -409,7 +409,8 @@ static __global__ void __launch_bounds__(256) lu_panel_cluster_kernel(T *P, long
 // part: 2 slots x G x (1 + NB) partial sums; x0buf: 2 slots.
 template <class T>
 static __global__ void __launch_bounds__(256) qr_panel_kernel(T *P, long long lda, int mrows, int kb, int rows_per, T *tau,
-                                                       T *part, T *x0buf, PanelSync *sync) {
+                                                       T *part, T *x0buf, PanelSync *sync,
+                                                       unsigned long long wait_ns) {
     constexpr int NB = PanelNB<T>::value;
     constexpr int LDR = NB + 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -443,7 +444,7 @@ static __global__ void __launch_bounds__(256) qr_panel_kernel(T *P, long long ld
             part[((size_t)slot * G + g) * PS] = t;
             if (j >= r0 && j < r1) x0buf[slot] = R[(j - r0) * LDR + j];
         }
-        if (!grid_barrier(&sync->ctr, (unsigned)(G * (++phase)), &sync->err)) return;
+        if (!grid_barrier(&sync->ctr, (unsigned)(G * (++phase)), &sync->err, wait_ns)) return;
         // sigma = sum of the CTAs' partials, a fixed tree over q (thread q, then warps)
         T sigma = T(0);
         for (int q = tid; q < G; q += blockDim.x) sigma += ((volatile T *)part)[((size_t)slot * G + q) * PS];
@@ -456,7 +457,7 @@ static __global__ void __launch_bounds__(256) qr_panel_kernel(T *P, long long ld
         const T x0 = ((volatile T *)x0buf)[slot];
         if (sigma == T(0)) {  // already a multiple of e1: tau = 0, nothing changes
             if (g == 0 && tid == 0) tau[j] = T(0);
-            if (!grid_barrier(&sync->ctr, (unsigned)(G * (++phase)), &sync->err)) return;
+            if (!grid_barrier(&sync->ctr, (unsigned)(G * (++phase)), &sync->err, wait_ns)) return;
             continue;
         }
         const T x_norm = sqrt(x0 * x0 + sigma);
@@ -475,7 +476,7 @@ static __global__ void __launch_bounds__(256) qr_panel_kernel(T *P, long long ld
             acc = warp_sum(acc);
             if (lane == 0) part[((size_t)slot * G + g) * PS + 1 + c] = acc;
         }
-        if (!grid_barrier(&sync->ctr, (unsigned)(G * (++phase)), &sync->err)) return;
+        if (!grid_barrier(&sync->ctr, (unsigned)(G * (++phase)), &sync->err, wait_ns)) return;
         // u_c = sum over CTAs of the partials: warp per column, lanes over CTAs
         for (int c = j + warp; c < kb; c += nw) {
             T a = T(0);
@@ -790,13 +791,16 @@ static __global__ void __launch_bounds__(128) trsm_diag_kernel(const T *D, long 
 // reciprocals) and publishes its rows. A CTA waits only on tickets taken before its own,
 // by CTAs that are running, so the sweep always progresses; a waiting thread sleeps
 // between polls (other streams' kernels share the SMs), and every wait is bounded by
-// kBarrierTimeoutNs (RL_ERR_TIMEOUT).
+// wait_ns (RL_TUNE_WAIT_TIMEOUT_NS; RL_ERR_TIMEOUT). withhold >= 0 is a test setting
+// (RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK): that block is solved but never published, so the
+// waits for it run out.
 // Per-launch state: ctl[0] = ticket, ctl[1 + b] = block b published, zeroed by the host.
 constexpr int kSweepRows = 64, kSweepRhs = 8, kSweepCtas = 32;
 template <class T>
 static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const T *__restrict__ A, long long lda, int n,
                                                              T *__restrict__ Y, long long ldy, int nrhs, int mode,
-                                                             int *ctl, int *status, T tiny) {
+                                                             int *ctl, int *status, T tiny,
+                                                             unsigned long long wait_ns, int withhold) {
     constexpr int BR = kSweepRows, LDD = BR + 1;
     __shared__ T Ds[BR * LDD];           // the diagonal block
     __shared__ T inv[BR];                 // 1 / d_ii
@@ -843,7 +847,7 @@ static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const T *__restr
             if (tid == 0 && !s_fail) {
                 const unsigned long long t0 = global_ns();
                 while (ld_acquire(ctl + 1 + k) == 0) {
-                    if (global_ns() - t0 > kBarrierTimeoutNs) {
+                    if (global_ns() - t0 > wait_ns) {
                         s_fail = 1;
                         break;
                     }
@@ -939,7 +943,8 @@ static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const T *__restr
         if (tid == 0) {
             if (s_fail) atomicCAS(status, 0, RL_ERR_TIMEOUT);
             __threadfence();
-            st_release(ctl + 1 + b, 1);  // published even after a timeout, so no later block waits forever
+            // published even after a timeout, so no later block waits forever
+            if (b != withhold) st_release(ctl + 1 + b, 1);
         }
     }
 }

@@ -136,7 +136,8 @@ rl_status lu_panel_cluster(T *P, long long lda, int mrows, int kb, int k0, int *
     constexpr int NB = PanelNB<T>::value;
     launched = false;
     auto kern = lu_panel_cluster_kernel<T>;
-    static const int cmax = probe_cluster(kern, kClusterSmem);
+    static const int cmax_hw = probe_cluster(kern, kClusterSmem);
+    const int cmax = std::min<int>(cmax_hw, (int)tune(RL_TUNE_PANEL_CLUSTER_MAX));
     const size_t row_bytes = (NB + 1) * sizeof(T), extra = (2 * 16 * NB + 2 * NB) * sizeof(T);
     int rows_per = 0;
     const int C = cluster_shape(mrows, row_bytes, extra, cmax, panel_target_rows<T>(), rows_per);
@@ -155,7 +156,8 @@ rl_status qr_panel_cluster(T *P, long long lda, int mrows, int kb, T *tau, cudaS
     constexpr int NB = PanelNB<T>::value;
     launched = false;
     auto kern = qr_panel_cluster_kernel<T>;
-    static const int cmax = probe_cluster(kern, kClusterSmem);
+    static const int cmax_hw = probe_cluster(kern, kClusterSmem);
+    const int cmax = std::min<int>(cmax_hw, (int)tune(RL_TUNE_PANEL_CLUSTER_MAX));
     const size_t row_bytes = (NB + 2) * sizeof(T), extra = (NB + 16 * NB + 16 + 1) * sizeof(T);
     int rows_per = 0;
     const int C = cluster_shape(mrows, row_bytes, extra, cmax, panel_target_rows<T>(), rows_per);
@@ -186,6 +188,7 @@ rl_status lu_factor_dev(T *A, long long lda, int n, int *ipiv, cudaStream_t s, T
     // launch) and read once at the end: a failed panel leaves identity pivots, the work
     // after it runs on in-range indices, and every later panel stops at its first barrier.
     RL_TRY_CUDA(cudaMemsetAsync(sync.p, 0, sizeof(PanelSync), s));
+    unsigned long long wns = wait_ns();
     for (int k0 = 0; k0 < n; k0 += NB) {
         const int kb = std::min(NB, n - k0), mrows = n - k0;
         int G, rows_per;
@@ -197,7 +200,8 @@ rl_status lu_factor_dev(T *A, long long lda, int n, int *ipiv, cudaStream_t s, T
         RL_TRY(lu_panel_cluster<T>(P, lda, mrows, kb, k0, ip, &sync.p->err, tiny, s, clustered));
         if (!clustered) {
             if (k0 > 0) RL_TRY_CUDA(cudaMemsetAsync(&sync.p->ctr, 0, sizeof(unsigned), s));
-            void *args[] = {&P, &lda, (void *)&mrows, (void *)&kb, &k0, &rows_per, &ip, &cand.p, &rowj.p, &sync.p, &tiny};
+            void *args[] = {&P,       &lda,   (void *)&mrows, (void *)&kb, &k0,  &rows_per,
+                            &ip,      &cand.p, &rowj.p,       &sync.p,     &tiny, &wns};
             RL_TRY(launch_coop<T>((void *)pk, G, smem, args, s));
         }
         const int nother = n - kb;
@@ -205,10 +209,9 @@ rl_status lu_factor_dev(T *A, long long lda, int n, int *ipiv, cudaStream_t s, T
             RL_TRY(laswp<T>(A, lda, n, k0, k0 + kb, ipiv, k0, k0 + kb, s));
         const int n2 = n - k0 - kb;
         if (n2 > 0) {
-            DevBuf<int> st;
-            RL_TRY(st.alloc(1, s));
-            RL_TRY_CUDA(cudaMemsetAsync(st.p, 0, sizeof(int), s));
-            RL_LAUNCH(trsm_diag_kernel<T>, ceil_div(n2, kTrsmCols), 128, 0, s, P, lda, kb, P + kb, lda, n2, 0, st.p, tiny);
+            // mode 0 (unit lower triangle) has no pivot to check: no status word
+            RL_LAUNCH(trsm_diag_kernel<T>, ceil_div(n2, kTrsmCols), 128, 0, s, P, lda, kb, P + kb, lda, n2, 0,
+                      (int *)nullptr, tiny);
             RL_TRY((gemm<T, false, false>(n2, n2, kb, T(-1), P + (long long)kb * lda, lda, P + kb, lda, T(1),
                                          P + (long long)kb * lda + kb, lda, s)));
         }
@@ -277,6 +280,7 @@ rl_status qr_factor_dev(T *A, long long lda, int m, int n, int nrefl, T *tau, cu
     RL_TRY(set_smem(pk, 200 * 1024));
     // Sticky error word, read once at the end (see lu_factor_dev).
     RL_TRY_CUDA(cudaMemsetAsync(sync.p, 0, sizeof(PanelSync), s));
+    unsigned long long wns = wait_ns();
     for (int k0 = 0; k0 < nrefl; k0 += NB) {
         const int kb = std::min(NB, nrefl - k0), mrows = m - k0;
         int G, rows_per;
@@ -288,7 +292,7 @@ rl_status qr_factor_dev(T *A, long long lda, int m, int n, int nrefl, T *tau, cu
         RL_TRY(qr_panel_cluster<T>(P, lda, mrows, kb, tk, s, clustered));
         if (!clustered) {
             if (k0 > 0) RL_TRY_CUDA(cudaMemsetAsync(&sync.p->ctr, 0, sizeof(unsigned), s));
-            void *args[] = {&P, &lda, (void *)&mrows, (void *)&kb, &rows_per, &tk, &part.p, &x0buf.p, &sync.p};
+            void *args[] = {&P, &lda, (void *)&mrows, (void *)&kb, &rows_per, &tk, &part.p, &x0buf.p, &sync.p, &wns};
             RL_TRY(launch_coop<T>((void *)pk, G, smem, args, s));
         }
         const int n2 = n - k0 - kb;
@@ -388,7 +392,7 @@ rl_status tri_solve_dev(const T *A, long long lda, int n, T *Y, long long ldy, i
         RL_TRY(ctl.alloc(1 + nb, s));
         RL_TRY_CUDA(cudaMemsetAsync(ctl.p, 0, sizeof(int) * (1 + nb), s));
         RL_LAUNCH(trsv_sweep_kernel<T>, std::min(nb, kSweepCtas), 256, 0, s, A, lda, n, Y, ldy, nrhs, mode, ctl.p, dstatus,
-                  tiny);
+                  tiny, wait_ns(), (int)tune(RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK));
         return RL_OK;
     }
     const int gr = ceil_div(nrhs, kTrsmCols);

@@ -37,7 +37,6 @@ constexpr int STAGE_BYTES = 4 * TILE_BYTES;    // A_hi, A_lo, B_hi, B_lo: 64 KB
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;  // + alignment slack + barriers
 constexpr int THREADS = 128;
 constexpr int TMEM_COLS = 128;
-constexpr unsigned long long kWaitLimit = 1ull << 26;  // polls of an mbarrier before giving up
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -74,10 +73,14 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
                  : "memory");
 }
 
-// Bounded wait for the given phase parity; false on expiry.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
+// Wait for the given phase parity, bounded by `limit` ns of %globaltimer (try_wait may
+// itself suspend the thread for a hardware-defined time, so a poll count would not bound
+// the wall time); false on expiry.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity, unsigned long long limit) {
     const uint32_t a = smem_u32(bar);
-    for (unsigned long long i = 0; i < kWaitLimit; i++) {
+    unsigned long long t0, t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    for (;;) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -87,8 +90,9 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
             : "r"(a), "r"(parity)
             : "memory");
         if (done) return true;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        if (t - t0 > limit) return false;
     }
-    return false;
 }
 
 // 2D tensor copy global -> shared (x = the K coordinate, y = the row), completing on bar.
@@ -172,7 +176,7 @@ static __global__ void __launch_bounds__(tc::THREADS, 1)
     sgemm_tma_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUtensorMap tAl,
                      const __grid_constant__ CUtensorMap tBh, const __grid_constant__ CUtensorMap tBl, int m, int n,
                      int kp, float alpha, float beta, float *__restrict__ C, long long ldc, int lower, int *err,
-                     int kc_per, long long zstride) {
+                     int kc_per, long long zstride, unsigned long long wait_ns) {
     using namespace tc;
     // lower: only the elements on or below the diagonal are written (the SYRK form);
     // tiles wholly above it do nothing
@@ -212,10 +216,11 @@ static __global__ void __launch_bounds__(tc::THREADS, 1)
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
 
+    int issued = 0;  // producer: chunks whose loads were issued
     if (warp == 0 && lane == 0) {  // producer
         for (int c = 0; c < nk; c++) {
             const int s = c % STAGES, use = c / STAGES;
-            if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1)) {
+            if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1, wait_ns)) {
                 s_fail = 1;
                 break;
             }
@@ -226,12 +231,13 @@ static __global__ void __launch_bounds__(tc::THREADS, 1)
             tma_load_2d(st + TILE_BYTES, &tAl, x, row0, &full[s]);
             tma_load_2d(st + 2 * TILE_BYTES, &tBh, x, col0, &full[s]);
             tma_load_2d(st + 3 * TILE_BYTES, &tBl, x, col0, &full[s]);
+            issued = c + 1;
         }
     } else if (warp == 1 && lane == 0) {  // MMA issuer
         constexpr uint32_t idesc = idesc_tf32(BM, BN);
         for (int c = 0; c < nk; c++) {
             const int s = c % STAGES, use = c / STAGES;
-            if (!mbar_wait(&full[s], use & 1)) {
+            if (!mbar_wait(&full[s], use & 1, wait_ns)) {
                 s_fail = 1;
                 break;
             }
@@ -252,8 +258,13 @@ static __global__ void __launch_bounds__(tc::THREADS, 1)
         mma_commit(done);
     }
     __syncwarp();
-    bool ok = nk == 0 || mbar_wait(done, 0);
+    bool ok = nk == 0 || mbar_wait(done, 0, wait_ns);  // every MMA issued (also after a failure) has completed
     ok = __syncthreads_and(ok && !s_fail) != 0;
+    if (!ok && warp == 0 && lane == 0) {
+        // Drain: the last load issued on each stage must land before this CTA's shared
+        // memory is given up (a wait that runs out here leaves nothing else to do).
+        for (int c = max(0, issued - STAGES); c < issued; c++) mbar_wait(&full[c % STAGES], (c / STAGES) & 1, wait_ns);
+    }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const int r = row0 + warp * 32 + lane;
 #pragma unroll 1
@@ -387,13 +398,13 @@ rl_status sgemm_tc(int m, int n, int k, float alpha, const float *A, long long l
         DevBuf<float> part;
         RL_TRY(part.alloc((size_t)grid.z * zstride, s));
         RL_LAUNCH(sgemm_tma_kernel, grid, tc::THREADS, tc::SMEM_BYTES, s, mAh, mAl, mBh, mBl, m, n, kp, 1.f, 0.f, part.p,
-                  (long long)n, 0, err, kc_per, zstride);
+                  (long long)n, 0, err, kc_per, zstride, wait_ns());
         RL_LAUNCH(splitk_reduce_kernel<float>, (int)std::min<long long>(4LL * num_sms(), (zstride + 255) / 256), 256, 0, s,
                   m, n, (int)grid.z, alpha, part.p, beta, C, ldc);
         return RL_OK;
     }
     RL_LAUNCH(sgemm_tma_kernel, grid, tc::THREADS, tc::SMEM_BYTES, s, mAh, mAl, mBh, mBl, m, n, kp, alpha, beta, C,
-              ldc, lower ? 1 : 0, err, nkc, 0ll);
+              ldc, lower ? 1 : 0, err, nkc, 0ll, wait_ns());
     return RL_OK;
 }
 

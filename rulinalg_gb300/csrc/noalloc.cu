@@ -114,6 +114,8 @@ extern "C" rl_status rl_dsolve_mixed_noalloc_dev(size_t n, int kind, const doubl
     d.iters_tag = 0;
     d.max_iters = 30;
     d.warp_small = 1;  // the order is largest-cost first
+    d.warp_cost = (int)tune(RL_TUNE_BATCH_WARP_COST);
+    d.wait_ns = wait_ns();
     RL_LAUNCH((batch_solve_kernel<double, float, true>), 1, CTA_THREADS, cta_smem_bytes<float>(), st, d, a, b, x);
 
     BatchDesc f = d;

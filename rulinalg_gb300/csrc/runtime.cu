@@ -65,6 +65,40 @@ int num_sms() {
     return g_num_sms > 0 ? g_num_sms : 152;
 }
 
+namespace {
+struct TuneKey {
+    int key;
+    int64_t lo, hi, value;
+};
+// Keys, ranges and defaults of the tunables (rulinalg_gb300.h documents each one).
+TuneKey g_tune_keys[] = {
+    {RL_TUNE_WAIT_TIMEOUT_NS, 1000000LL, 10000000000LL, 1000000000LL},
+    {RL_TUNE_PANEL_CLUSTER_MAX, 0, 16, 16},
+    {RL_TUNE_BATCH_CTAS_PER_SM, 0, 8, 0},
+    {RL_TUNE_BATCH_WARP_COST, 0, 32768, 32768},
+    {RL_TUNE_UPLOAD_CHUNKS, 1, 256, 32},
+    {RL_TUNE_TEST_WITHHOLD_CHUNK, -1, 255, -1},
+    {RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK, -1, 1LL << 30, -1},
+};
+constexpr int kTuneCount = sizeof(g_tune_keys) / sizeof(g_tune_keys[0]);
+std::atomic<int64_t> g_tune_values[kTuneCount];
+std::once_flag g_tune_once;
+void tune_init() {
+    for (int i = 0; i < kTuneCount; i++) g_tune_values[i].store(g_tune_keys[i].value);
+}
+int tune_index(int key) {
+    for (int i = 0; i < kTuneCount; i++)
+        if (g_tune_keys[i].key == key) return i;
+    return -1;
+}
+}  // namespace
+
+int64_t tune(int key) {
+    std::call_once(g_tune_once, tune_init);
+    const int i = tune_index(key);
+    return i < 0 ? 0 : g_tune_values[i].load(std::memory_order_relaxed);
+}
+
 }  // namespace rl
 
 extern "C" {
@@ -93,5 +127,20 @@ int rl_version(void) { return 100; }
 rl_status rl_device_check(void) { return rl::ensure_device(); }
 
 uint64_t rl_launch_count(void) { return rl::g_launches.load(std::memory_order_relaxed); }
+
+rl_status rl_tune_set(int key, int64_t value) {
+    std::call_once(rl::g_tune_once, rl::tune_init);
+    const int i = rl::tune_index(key);
+    if (i < 0 || value < rl::g_tune_keys[i].lo || value > rl::g_tune_keys[i].hi) return RL_ERR_INVALID_ARG;
+    rl::g_tune_values[i].store(value);
+    return RL_OK;
+}
+
+rl_status rl_tune_get(int key, int64_t *value) {
+    const int i = rl::tune_index(key);
+    if (i < 0 || !value) return RL_ERR_INVALID_ARG;
+    *value = rl::tune(key);
+    return RL_OK;
+}
 
 }  // extern "C"

@@ -48,6 +48,7 @@ struct Resident {
     std::unique_ptr<MixedFactor> f;
     std::mutex mu;  // solves against one factor are serialised (the FP64 fallback is built lazily)
     size_t bytes = 0;
+    bool released = false;  // set under mu by rl_server_release_factor; a queued re-solve then fails
 };
 
 }  // namespace
@@ -220,6 +221,8 @@ struct Worker {
         d.iters_tag = 0;
         d.max_iters = 30;
         d.warp_small = 1;  // the order is largest-cost first
+    d.warp_cost = (int)tune(RL_TUNE_BATCH_WARP_COST);
+    d.wait_ns = wait_ns();
         RL_LAUNCH((batch_solve_kernel<double, float, true>), std::min(grid32, B), CTA_THREADS, smem32, st, d, dA.p,
                   dB.p, dX.p);
         BatchDesc f = d;
@@ -302,6 +305,8 @@ struct Worker {
             res = it->second;
         }
         std::lock_guard<std::mutex> lk(res->mu);
+        // released between the lookup and this lock: its device buffers are gone
+        if (res->released) return RL_ERR_INVALID_ARG;
         if (q->r.n != (size_t)res->f->n) return RL_ERR_SHAPE;
         q->res.factor = q->r.factor;
         return solve_with(*res->f, q);
@@ -521,6 +526,7 @@ rl_status rl_server_release_factor(rl_server *s, uint64_t factor) {
         std::lock_guard<std::mutex> lk(res->mu);  // no solve in flight on it any more
         cudaStreamSynchronize(res->f->home);
         res->f->release();
+        res->released = true;
     }
     std::lock_guard<std::mutex> lk(s->mu);
     s->bytes_in_use -= std::min(s->bytes_in_use, res->bytes);

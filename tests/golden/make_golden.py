@@ -6,7 +6,7 @@ test sources: this script reads the `matrix![..]`, `vector![..]` and `vec![..]` 
 and writes them, with their citations, as a JSON fixture. Run it where the reference is
 present:
 
-    python tests/golden/make_golden.py [/path/to/rulinalg]
+    python tests/golden/make_golden.py /path/to/rulinalg
 
 The fixture is committed; tests never read the reference tree.
 """
@@ -146,4 +146,6 @@ def main(ref: Path) -> None:
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference"))
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: python tests/golden/make_golden.py <path of the rulinalg 0.4.2 source tree>")
+    main(Path(sys.argv[1]))

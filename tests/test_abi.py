@@ -55,3 +55,23 @@ def test_no_device_fails_loudly(rl):
         rl.mat_mul(a, a)
     with pytest.raises(rl.DeviceError):
         rl.PartialPivLu.decompose(a)
+
+
+def test_tunables_ranges_and_defaults(rl):
+    """rl_tune_set / rl_tune_get need no GPU: defaults, range checks, unknown keys."""
+    from rulinalg_gb300 import _lib as L
+    defaults = {L.TUNE_WAIT_TIMEOUT_NS: 10 ** 9, L.TUNE_PANEL_CLUSTER_MAX: 16, L.TUNE_BATCH_CTAS_PER_SM: 0,
+                L.TUNE_BATCH_WARP_COST: 32768, L.TUNE_UPLOAD_CHUNKS: 32, L.TUNE_TEST_WITHHOLD_CHUNK: -1,
+                L.TUNE_TEST_WITHHOLD_SWEEP_BLOCK: -1}
+    for k, v in defaults.items():
+        assert rl.tune_get(k) == v
+    import pytest
+    for k, bad in ((L.TUNE_WAIT_TIMEOUT_NS, 0), (L.TUNE_PANEL_CLUSTER_MAX, 17), (L.TUNE_UPLOAD_CHUNKS, 0),
+                   (L.TUNE_BATCH_WARP_COST, 40000), (L.TUNE_TEST_WITHHOLD_CHUNK, -2), (999, 1)):
+        with pytest.raises(ValueError):
+            rl.tune_set(k, bad)
+    rl.tune_set(L.TUNE_UPLOAD_CHUNKS, 7)
+    assert rl.tune_get(L.TUNE_UPLOAD_CHUNKS) == 7
+    rl.tune_set(L.TUNE_UPLOAD_CHUNKS, 32)
+    for k, v in defaults.items():
+        assert rl.tune_get(k) == v

@@ -6,6 +6,8 @@ the oracle's pivot choice is unique by a margin, factors normwise close, every s
 normwise backward error <= n 2^-53 10 (f64) and forward error reported against the
 oracle. Known answers use the reference's comparators.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -98,6 +100,44 @@ def test_gemm_k_zero_and_empty(gpu):
     assert gpu.mat_mul(np.zeros((0, 5)), np.zeros((5, 2))).shape == (0, 2)
     with pytest.raises(gpu.RulinalgPanic):
         gpu.mat_mul(np.zeros((2, 3)), np.zeros((2, 3)))
+
+
+THREADS = os.cpu_count() or 1
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("n", [1024, 2048, 4096])
+def test_gemm_config2_against_oracle(gpu, dtype, n):
+    """The dense GEMM sweep's sizes (N(0,1), seeded, row-major): normwise
+    ||C - C_ref||_F <= n eps ||A||_F ||B||_F against the oracle's f64 product of the same
+    (type-rounded) inputs, the oracle's rows split over all host threads."""
+    from rulinalg_gb300.workloads import gemm_operands
+    a, b = gemm_operands(n, dtype, seed=n)
+    got = gpu.mat_mul(a, b).astype(np.float64)
+    ref = O.gemm(a.astype(np.float64), b.astype(np.float64), threads=THREADS)
+    eps = U64 if dtype == np.float64 else U32
+    err, bound = fro(got - ref), n * eps * fro(a) * fro(b)
+    print(f"gemm n={n} {np.dtype(dtype).name}: ||C - C_ref||_F / bound = {err / bound:.3e}")
+    assert err <= bound
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_gemm_config2_8192(gpu, dtype):
+    """n = 8192, the sweep's largest size: the oracle's scalar i-k-j loop would be 1.1
+    TFLOP of scalar work (many minutes on the host), so the reference product here is an
+    FP64 product on the GPU (torch / cuBLAS DGEMM, error ~ sqrt(n) 2^-53 |A||B|, far inside
+    the bound), against the same normwise bound n eps ||A||_F ||B||_F."""
+    import torch
+    from rulinalg_gb300.workloads import gemm_operands
+    n = 8192
+    a, b = gemm_operands(n, dtype, seed=n)
+    got = gpu.mat_mul(a, b).astype(np.float64)
+    dev = torch.device("cuda:0")
+    ref = (torch.from_numpy(a.astype(np.float64)).to(dev) @ torch.from_numpy(b.astype(np.float64)).to(dev)).cpu().numpy()
+    eps = U64 if dtype == np.float64 else U32
+    err, bound = fro(got - ref), n * eps * fro(a) * fro(b)
+    print(f"gemm n={n} {np.dtype(dtype).name}: ||C - C_ref||_F / bound = {err / bound:.3e}")
+    assert err <= bound
 
 
 def test_gemm_large_linearity(gpu):
@@ -193,15 +233,34 @@ def test_lu_parity_random(gpu, n):
     assert np.max(np.abs(x - xo)) <= 1e-9 * max(np.max(np.abs(xo)), 1)
 
 
+def unique_max_by_construction(n, rng, dtype):
+    """A = P^T L U with L unit lower triangular, |l_ij| <= 1/(2 sqrt(n)), and a random
+    row permutation P: at every elimination step the candidates of the pivot column are
+    u_kk l_ik, so partial pivoting must take the row holding l_kk = 1, by a margin of
+    about |u_kk| (1 - 1/(2 sqrt(n))). The off-diagonal scale keeps ||L - I||_2 below 1/2
+    (L and U well conditioned), so FP32 rounding of A cannot move a multiplier far
+    enough to close that margin. The tests check the oracle's gaps."""
+    c = 0.5 / np.sqrt(max(n, 1))
+    l = np.tril(rng.uniform(-c, c, (n, n)), -1) + np.eye(n)
+    u = np.triu(rng.uniform(-2 * c, 2 * c, (n, n)), 1) + np.diag(rng.uniform(1.0, 2.0, n) * rng.choice([-1, 1], n))
+    p = rng.permutation(n)
+    a = np.empty((n, n))
+    a[p] = l @ u  # row i of L U lands at row p[i]
+    return a.astype(dtype)
+
+
 def test_lu_f32_parity(gpu):
+    """FP32 PartialPivLu: pivots bit-identical to the oracle's on inputs with a unique
+    column maximum at every step (asserted for every size), factors and solves checked."""
     rng = np.random.default_rng(3)
-    for n in (9, 100, 300, 700):
-        a = (rng.uniform(-1.0, 1.0, (n, n)) + np.eye(n)).astype(np.float32)
-        _, operm, st, gap = O.lu_decompose(a, gaps=True)
+    for n in (9, 100, 300, 700, 1500):
+        a = unique_max_by_construction(n, rng, np.float32)
+        olu, operm, st, gap = O.lu_decompose(a, gaps=True)
+        assert st == O.OK and (n < 2 or gap[:-1].min() > 0.3)
         lu = gpu.PartialPivLu.decompose(a)
         assert lu.lu.dtype == np.float32
-        if n < 2 or gap[:-1].min() > 1e-4:  # pivots compared where the choice is unique
-            assert np.array_equal(lu.p.perm, operm)
+        assert np.array_equal(lu.p.perm, operm), n
+        assert fro(np.triu(lu.lu) - np.triu(olu)) <= 10 * n * U32 * fro(np.triu(olu))
         b = rng.uniform(-1, 1, n).astype(np.float32)
         x = lu.solve(b)
         assert backward_error(a, x, b) <= n * U32 * 10
@@ -373,3 +432,37 @@ def test_qr_f32_against_f64_oracle(gpu, m, n):
     assert np.max(np.abs(h.tau.astype(np.float64) - otau)) <= 50 * n * eps32
     r32 = np.triu(h.qr.astype(np.float64))[:n]
     assert fro(r32 - np.triu(oqr)[:n]) <= 10 * n * eps32 * fro(a)
+
+
+# ---------------------------------------------- cooperative-grid panels (tunable) --
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_lu_and_qr_cooperative_panels(gpu, dtype):
+    """RL_TUNE_PANEL_CLUSTER_MAX = 0 sends every blocked LU / QR panel to the
+    cooperative-grid kernels (lu_panel_kernel, qr_panel_kernel), which otherwise run only
+    for panels too tall for a 16-CTA cluster (FP64 m > ~6,300): pivots bit-identical to
+    the oracle on unique-maximum inputs, factors and solves checked, then the default
+    restored and the cluster path checked to give the same pivots."""
+    from rulinalg_gb300 import _lib as L
+    rng = np.random.default_rng(77)
+    n = 1100
+    a = unique_max_by_construction(n, rng, dtype) if dtype == np.float32 else unique_pivot_input(n, rng)
+    b = rng.uniform(-1, 1, n).astype(dtype)
+    olu, operm, st = O.lu_decompose(a, threads=THREADS)
+    m_qr, n_qr = 1300, 600
+    aq = rng.standard_normal((m_qr, n_qr)).astype(dtype)
+    oqr, otau = O.qr_decompose(aq.astype(np.float64))
+    eps = U64 if dtype == np.float64 else U32
+    gpu.tune_set(L.TUNE_PANEL_CLUSTER_MAX, 0)
+    try:
+        lu = gpu.PartialPivLu.decompose(a)
+        x = lu.solve(b)
+        h = gpu.HouseholderQr.decompose(aq)
+    finally:
+        gpu.tune_set(L.TUNE_PANEL_CLUSTER_MAX, 16)
+    assert np.array_equal(lu.p.perm, operm)
+    assert fro(np.triu(lu.lu) - np.triu(olu)) <= 10 * n * eps * fro(np.triu(olu))
+    assert backward_error(a, x, b) <= n * eps * 10
+    assert np.max(np.abs(h.tau.astype(np.float64) - otau)) <= 50 * n_qr * eps
+    assert fro(np.triu(h.qr.astype(np.float64))[:n_qr] - np.triu(oqr)[:n_qr]) <= 10 * n_qr * eps * fro(aq)
+    lu2 = gpu.PartialPivLu.decompose(a)  # default: cluster panels
+    assert np.array_equal(lu2.p.perm, operm)

@@ -88,6 +88,39 @@ def test_resident_factor_resolves(gpu, server):
         server.submit(3, b=rng.standard_normal(600), factor=h)
 
 
+def test_release_while_resolves_are_queued(gpu, server):
+    """A factor released while re-solves against it are queued or running: every
+    re-solve either completes (f64-accurate) or reports InvalidArg (the factor was gone
+    by the time a worker held it); none runs on freed device memory."""
+    rng = np.random.default_rng(21)
+    n = 900
+    a, b = system(rng, 0, n)
+    t, _ = server.submit(0, a, b, retain=True)
+    h = server.wait(t)["factor"]
+    rhs = [rng.standard_normal(n) for _ in range(40)]
+    tickets = [server.submit(3, b=r, factor=h)[0] for r in rhs]
+    server.release_factor(h)
+    done = failed = 0
+    for tk, r in zip(tickets, rhs):
+        try:
+            res = server.wait(tk)
+        except gpu.RulinalgError as e:
+            assert e.kind == "InvalidArg"
+            failed += 1
+            continue
+        if res["status"] == 0:
+            assert backward_error(a, res["x"], r) <= n * U64 * 10
+            done += 1
+        else:
+            assert res["status"] == 1, res  # RL_ERR_INVALID_ARG
+            failed += 1
+    assert done + failed == len(rhs)
+    print(f"re-solves completed before the release: {done}, refused after it: {failed}")
+    # the server is still healthy
+    t, _ = server.submit(0, a, b)
+    assert backward_error(a, server.wait(t)["x"], b) <= n * U64 * 10
+
+
 def test_admission_by_footprint(gpu):
     n = 1500  # ~27 MB of footprint each
     srv = gpu.Server(hbm_budget_bytes=64 << 20, workers=4)
