@@ -249,8 +249,10 @@ def test_config4_full_size(gpu):
         hb = host_berr(ab, bb, xb)
         k = int(n[idx[0]])
         assert np.all(hb <= k * U64 * 10), (k, hb.max())
-        # device-reported backward errors are the solutions' own
-        assert np.all(bm[idx] <= 10 * hb + U64 * 1e-2) and np.all(hb <= 10 * bm[idx] + U64 * 1e-2)
+        # device-reported backward errors are the solutions' own (two FP64 evaluations of
+        # a residual at the rounding floor differ by up to ~sqrt(n) u relative)
+        slack = 4 * np.sqrt(k) * U64
+        assert np.all(bm[idx] <= 10 * hb + slack) and np.all(hb <= 10 * bm[idx] + slack)
         xob = np.stack([xo[b_off[i]:b_off[i + 1]] for i in idx])
         ho = host_berr(ab, bb, xob)
         fe = np.max(np.abs(xb - xob), 1) / np.max(np.abs(xob), 1)
