@@ -51,6 +51,7 @@ typedef int rl_status;
 #define RL_ERR_OUT_OF_MEMORY 34
 #define RL_ERR_TIMEOUT 35
 #define RL_ERR_NOT_CONVERGED 36
+#define RL_ERR_BUSY 37 /* the serving loop's queue is full (backpressure); submit again later */
 
 /* Human-readable text for a status (static storage). */
 RL_API const char *rl_status_string(rl_status status);
@@ -272,6 +273,8 @@ typedef struct rl_server_config {
     int workers;             /* worker threads / CUDA streams (0: 8); worker 0 serves only batchable requests */
     int max_batch;           /* systems per batched launch (0: 4096) */
     int small_n;             /* largest n sent to the batched kernel (0: 512) */
+    int max_pending;         /* requests submitted but not finished, at most (0: no limit); beyond it
+                                rl_server_submit returns RL_ERR_BUSY and counts a rejection */
 } rl_server_config;
 typedef struct rl_request {
     int kind;        /* RL_REQ_* */
@@ -296,9 +299,11 @@ typedef struct rl_server_stats {
     uint64_t submitted, completed, failed, batches, batched_requests;
     uint64_t bytes_in_use, bytes_peak, bytes_budget, resident_factors;
     double p50_us, p99_us, mean_us, solves_per_s;
+    uint64_t rejected; /* submissions refused with RL_ERR_BUSY */
 } rl_server_stats;
 RL_API rl_status rl_server_create(const rl_server_config *cfg, rl_server **server);
-/* Non-blocking; RL_ERR_OUT_OF_MEMORY when the request can never fit the budget. */
+/* Non-blocking; RL_ERR_OUT_OF_MEMORY when the request can never fit the budget, RL_ERR_BUSY
+ * when max_pending requests are already in the server. */
 RL_API rl_status rl_server_submit(rl_server *server, const rl_request *req, uint64_t *ticket);
 /* Blocks until the ticket completes (timeout_s < 0: no limit); the ticket is consumed. */
 RL_API rl_status rl_server_wait(rl_server *server, uint64_t ticket, double timeout_s, rl_result *result);
@@ -306,7 +311,8 @@ RL_API rl_status rl_server_release_factor(rl_server *server, uint64_t factor);
 RL_API rl_status rl_server_stats_get(rl_server *server, rl_server_stats *stats);
 RL_API rl_status rl_server_reset_stats(rl_server *server);
 /* Load replay: submits reqs[i] at arrival_s[i] seconds after the call (a Poisson trace,
- * say), then waits for all of them; results[i] receives each outcome. */
+ * say), then waits for all of them; results[i] receives each outcome (status
+ * RL_ERR_BUSY for a request refused by backpressure). */
 RL_API rl_status rl_server_replay(rl_server *server, size_t count, const double *arrival_s, const rl_request *reqs,
                                   rl_result *results);
 /* Drains the admitted requests, releases resident factors and stops the workers. */

@@ -97,7 +97,8 @@ SIGNATURES = {
 
 class ServerConfig(C.Structure):
     """rl_server_config"""
-    _fields_ = [("hbm_budget_bytes", C.c_size_t), ("workers", C.c_int), ("max_batch", C.c_int), ("small_n", C.c_int)]
+    _fields_ = [("hbm_budget_bytes", C.c_size_t), ("workers", C.c_int), ("max_batch", C.c_int), ("small_n", C.c_int),
+                ("max_pending", C.c_int)]
 
 
 class Request(C.Structure):
@@ -117,7 +118,18 @@ class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64), ("batches", C.c_uint64),
                 ("batched_requests", C.c_uint64), ("bytes_in_use", C.c_uint64), ("bytes_peak", C.c_uint64),
                 ("bytes_budget", C.c_uint64), ("resident_factors", C.c_uint64), ("p50_us", C.c_double),
-                ("p99_us", C.c_double), ("mean_us", C.c_double), ("solves_per_s", C.c_double)]
+                ("p99_us", C.c_double), ("mean_us", C.c_double), ("solves_per_s", C.c_double),
+                ("rejected", C.c_uint64)]
+
+
+# numpy layouts of rl_request and rl_result, for request streams built without a Python
+# loop (Server.replay_arrays)
+import numpy as _np  # noqa: E402
+REQUEST_DTYPE = _np.dtype([("kind", "<i4"), ("retain", "<i4"), ("factor", "<u8"), ("m", "<u8"), ("n", "<u8"),
+                           ("a", "<u8"), ("b", "<u8"), ("x", "<u8")])
+RESULT_DTYPE = _np.dtype([("status", "<i4"), ("iters", "<i4"), ("path", "<i4"), ("reserved", "<i4"),
+                          ("berr", "<f8"), ("factor", "<u8"), ("queue_us", "<f8"), ("latency_us", "<f8")])
+assert REQUEST_DTYPE.itemsize == C.sizeof(Request) and RESULT_DTYPE.itemsize == C.sizeof(Result)
 
 
 class SolveInfo(C.Structure):

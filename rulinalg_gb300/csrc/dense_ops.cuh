@@ -167,8 +167,28 @@ rl_status qr_panel_cluster(T *P, long long lda, int mrows, int kb, T *tau, cudaS
     return RL_OK;
 }
 
+// op(A) Y = Y' in place (triangular solve; modes and paths at the definition below).
+template <class T>
+rl_status tri_solve_dev(const T *A, long long lda, int n, T *Y, long long ldy, int nrhs, int mode, int *dstatus,
+                        cudaStream_t s, T tiny = Eps<T>::value);
+
+// Outer block width of the blocked factorisations. FP32 (the mixed-precision factor and
+// Matrix<f32>): 256-column blocks, each factored with the 64-column panels confined to
+// the block, then ONE trailing update of K = 256 on the tensor cores (tcgen05, 3xTF32;
+// the K = 64 updates of the inner panels measured slower there and stay on the SIMT
+// kernel). FP64: 0, one block spanning the matrix (every update is a K = 64 DFMA GEMM,
+// already at the FP64 rate).
+template <class T>
+constexpr int outer_nb() {
+    return std::is_same<T, float>::value ? 256 : 0;
+}
+
 // Blocked right-looking LU for any n: panel (one cluster, or a cooperative grid for
-// panels too tall for a cluster), row swaps, U12 solve, GEMM.
+// panels too tall for a cluster), row swaps, U12 solve, GEMM. Within an outer block the
+// swaps, U12 solves and updates of each 64-column panel cover the block's columns only;
+// the block's swaps reach the other columns afterwards (LAPACK's getrf order), then
+// U12 = L11^-1 A12 and A22 -= L21 U12 with K = the block width. The pivots are those of
+// partial pivoting over the whole column either way.
 template <class T>
 rl_status lu_factor_dev(T *A, long long lda, int n, int *ipiv, cudaStream_t s, T tiny = Eps<T>::value) {
     if (n <= 0) return RL_OK;
@@ -189,31 +209,46 @@ rl_status lu_factor_dev(T *A, long long lda, int n, int *ipiv, cudaStream_t s, T
     // after it runs on in-range indices, and every later panel stops at its first barrier.
     RL_TRY_CUDA(cudaMemsetAsync(sync.p, 0, sizeof(PanelSync), s));
     unsigned long long wns = wait_ns();
-    for (int k0 = 0; k0 < n; k0 += NB) {
-        const int kb = std::min(NB, n - k0), mrows = n - k0;
-        int G, rows_per;
-        panel_geometry<T>(mrows, G, rows_per);
-        const size_t smem = ((size_t)rows_per * (NB + 1) + NB) * sizeof(T);
-        T *P = A + (long long)k0 * lda + k0;
-        int *ip = ipiv + k0;
-        bool clustered = false;
-        RL_TRY(lu_panel_cluster<T>(P, lda, mrows, kb, k0, ip, &sync.p->err, tiny, s, clustered));
-        if (!clustered) {
-            if (k0 > 0) RL_TRY_CUDA(cudaMemsetAsync(&sync.p->ctr, 0, sizeof(unsigned), s));
-            void *args[] = {&P,       &lda,   (void *)&mrows, (void *)&kb, &k0,  &rows_per,
-                            &ip,      &cand.p, &rowj.p,       &sync.p,     &tiny, &wns};
-            RL_TRY(launch_coop<T>((void *)pk, G, smem, args, s));
+    const int NBO = outer_nb<T>() > 0 ? outer_nb<T>() : n;
+    for (int K0 = 0; K0 < n; K0 += NBO) {
+        const int K1 = std::min(n, K0 + NBO), KB = K1 - K0;
+        for (int k0 = K0; k0 < K1; k0 += NB) {
+            const int kb = std::min(NB, K1 - k0), mrows = n - k0;
+            int G, rows_per;
+            panel_geometry<T>(mrows, G, rows_per);
+            const size_t smem = ((size_t)rows_per * (NB + 1) + NB) * sizeof(T);
+            T *P = A + (long long)k0 * lda + k0;
+            int *ip = ipiv + k0;
+            bool clustered = false;
+            RL_TRY(lu_panel_cluster<T>(P, lda, mrows, kb, k0, ip, &sync.p->err, tiny, s, clustered));
+            if (!clustered) {
+                if (k0 > 0) RL_TRY_CUDA(cudaMemsetAsync(&sync.p->ctr, 0, sizeof(unsigned), s));
+                void *args[] = {&P,       &lda,   (void *)&mrows, (void *)&kb, &k0,  &rows_per,
+                                &ip,      &cand.p, &rowj.p,       &sync.p,     &tiny, &wns};
+                RL_TRY(launch_coop<T>((void *)pk, G, smem, args, s));
+            }
+            // the swaps in the block's other columns (every other column for one block)
+            RL_TRY(laswp<T>(A + K0, lda, KB, k0 - K0, k0 - K0 + kb, ipiv, k0, k0 + kb, s));
+            const int n2 = K1 - k0 - kb, m2 = mrows - kb;
+            if (n2 > 0) {
+                // mode 0 (unit lower triangle) has no pivot to check: no status word
+                RL_LAUNCH(trsm_diag_kernel<T>, ceil_div(n2, kTrsmCols), 128, 0, s, P, lda, kb, P + kb, lda, n2, 0,
+                          (int *)nullptr, tiny);
+                RL_TRY((gemm<T, false, false>(m2, n2, kb, T(-1), P + (long long)kb * lda, lda, P + kb, lda, T(1),
+                                             P + (long long)kb * lda + kb, lda, s)));
+            }
         }
-        const int nother = n - kb;
-        if (nother > 0)
-            RL_TRY(laswp<T>(A, lda, n, k0, k0 + kb, ipiv, k0, k0 + kb, s));
-        const int n2 = n - k0 - kb;
-        if (n2 > 0) {
-            // mode 0 (unit lower triangle) has no pivot to check: no status word
-            RL_LAUNCH(trsm_diag_kernel<T>, ceil_div(n2, kTrsmCols), 128, 0, s, P, lda, kb, P + kb, lda, n2, 0,
-                      (int *)nullptr, tiny);
-            RL_TRY((gemm<T, false, false>(n2, n2, kb, T(-1), P + (long long)kb * lda, lda, P + kb, lda, T(1),
-                                         P + (long long)kb * lda + kb, lda, s)));
+        if (K1 < n) {
+            // the block's swaps in the columns left and right of it, then U12 and the
+            // K = KB trailing update (tensor cores for FP32)
+            RL_TRY(laswp<T>(A, lda, n, K0, K1, ipiv, K0, K1, s));
+            const int N2 = n - K1;
+            T *L11 = A + (long long)K0 * lda + K0;
+            RL_TRY(tri_solve_dev<T>(L11, lda, KB, L11 + KB, lda, N2, 0, &sync.p->err, s, tiny));
+            RL_TRY((gemm<T, false, false>(N2, N2, KB, T(-1), L11 + (long long)KB * lda, lda, L11 + KB, lda, T(1),
+                                         L11 + (long long)KB * lda + KB, lda, s)));
+        } else if (K0 > 0) {
+            RL_TRY(laswp<T>(A, lda, K0, 0, 0, ipiv, K0, K1, s));  // the last block's swaps on the left
         }
     }
     int err = 0;
@@ -223,10 +258,38 @@ rl_status lu_factor_dev(T *A, long long lda, int n, int *ipiv, cudaStream_t s, T
 }
 
 // Blocked right-looking Cholesky: diagonal block by one CTA, L21 = A21 L11^-T, SYRK.
+// FP32: 256-column blocks (outer_nb); L11^-1 comes from a triangular solve with the
+// identity, L21 = A21 (L11^-1)^T and the lower-triangle SYRK A22 -= L21 L21^T (K = 256)
+// run on the tensor cores. FP64: 64-column blocks, L21 by substitution, DFMA SYRK. The
+// strict upper triangle is never written either way.
 template <class T>
 rl_status chol_factor_dev(T *A, long long lda, int n, cudaStream_t s, T tiny = Eps<T>::value) {
     if (n <= 0) return RL_OK;
     if (n <= CTA_NMAX) return factor_small<T>(A, lda, n, 1, nullptr, s, tiny);
+    if constexpr (outer_nb<T>() > 0) {
+        constexpr int NBO = outer_nb<T>();
+        DevBuf<T> Linv, T21;
+        DevBuf<int> st;
+        RL_TRY(Linv.alloc((size_t)NBO * NBO, s));
+        RL_TRY(T21.alloc((size_t)(n - std::min(n, NBO)) * NBO, s));
+        RL_TRY(st.alloc(1, s));
+        RL_TRY_CUDA(cudaMemsetAsync(st.p, 0, sizeof(int), s));
+        for (int K0 = 0; K0 < n; K0 += NBO) {
+            const int KB = std::min(NBO, n - K0), m2 = n - K0 - KB;
+            T *P = A + (long long)K0 * lda + K0;
+            RL_TRY(factor_small<T>(P, lda, KB, 1, nullptr, s, tiny));
+            if (m2 <= 0) continue;
+            const long long kk = (long long)KB * KB;
+            RL_LAUNCH(eye_kernel<T>, (int)((kk + 255) / 256), 256, 0, s, Linv.p, (long long)KB, KB, KB);
+            RL_TRY(tri_solve_dev<T>(P, lda, KB, Linv.p, KB, KB, 1, st.p, s, tiny));
+            T *A21 = P + (long long)KB * lda;
+            RL_TRY((gemm<T, false, true>(m2, KB, KB, T(1), A21, lda, Linv.p, KB, T(0), T21.p, KB, s)));
+            RL_TRY_CUDA(cudaMemcpy2DAsync(A21, lda * sizeof(T), T21.p, KB * sizeof(T), KB * sizeof(T), m2,
+                                          cudaMemcpyDeviceToDevice, s));
+            RL_TRY((gemm<T, false, true, true>(m2, m2, KB, T(-1), A21, lda, A21, lda, T(1), A21 + KB, lda, s)));
+        }
+        return read_status<T>(st.p, s);
+    }
     constexpr int NB = PanelNB<T>::value;
     for (int k0 = 0; k0 < n; k0 += NB) {
         const int kb = std::min(NB, n - k0), mrows = n - k0;
@@ -348,7 +411,7 @@ rl_status qr_first_k_dev(const T *QR, long long lda, int m, int n, const T *tau,
 // recorded as RL_ERR_DIV_BY_ZERO in *dstatus.
 template <class T>
 rl_status tri_solve_dev(const T *A, long long lda, int n, T *Y, long long ldy, int nrhs, int mode, int *dstatus,
-                        cudaStream_t s, T tiny = Eps<T>::value) {
+                        cudaStream_t s, T tiny) {
     if (n <= 0 || nrhs <= 0) return RL_OK;
     constexpr int NB = 64;
     if (nrhs <= kSweepRhs && g_shared_gpu) {

@@ -118,6 +118,7 @@ const char *rl_status_string(rl_status s) {
         case RL_ERR_OUT_OF_MEMORY: return "out of device memory";
         case RL_ERR_TIMEOUT: return "device wait timed out";
         case RL_ERR_NOT_CONVERGED: return "iterative refinement did not converge";
+        case RL_ERR_BUSY: return "server queue full (backpressure)";
         default: return "unknown status";
     }
 }

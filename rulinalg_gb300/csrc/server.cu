@@ -70,7 +70,8 @@ struct rl_server {
     void (*free_workers)(void *) = nullptr;  // destroys it (streams, slots)
     // statistics
     std::vector<double> lat_us;
-    uint64_t submitted = 0, completed = 0, failed = 0, batches = 0, batched = 0;
+    uint64_t submitted = 0, completed = 0, failed = 0, batches = 0, batched = 0, rejected = 0;
+    size_t in_server = 0;  // submitted and not finished (the backpressure count)
     double t_first = -1, t_last = 0;
 };
 
@@ -115,6 +116,7 @@ void finish(rl_server &s, Req *q, rl_status st) {
     q->res.queue_us = q->t_start - q->t_submit;
     q->res.latency_us = q->t_done - q->t_submit;
     q->done = true;
+    s.in_server--;
     s.lat_us.push_back(q->res.latency_us);
     s.completed++;
     if (st != RL_OK) s.failed++;
@@ -483,6 +485,12 @@ rl_status rl_server_submit(rl_server *s, const rl_request *req, uint64_t *ticket
         delete q;
         return RL_ERR_INVALID_ARG;
     }
+    if (s->cfg.max_pending > 0 && s->in_server >= (size_t)s->cfg.max_pending) {
+        delete q;
+        s->rejected++;
+        return RL_ERR_BUSY;
+    }
+    s->in_server++;
     q->batchable = is_batchable(*s, q->r);
     q->id = s->next_id++;
     q->t_submit = now_us();
@@ -544,6 +552,7 @@ rl_status rl_server_stats_get(rl_server *s, rl_server_stats *st) {
     st->failed = s->failed;
     st->batches = s->batches;
     st->batched_requests = s->batched;
+    st->rejected = s->rejected;
     st->bytes_in_use = s->bytes_in_use;
     st->bytes_peak = s->bytes_peak;
     st->bytes_budget = s->budget;
@@ -565,7 +574,7 @@ rl_status rl_server_reset_stats(rl_server *s) {
     if (!s) return RL_ERR_INVALID_ARG;
     std::lock_guard<std::mutex> lk(s->mu);
     s->lat_us.clear();
-    s->submitted = s->completed = s->failed = s->batches = s->batched = 0;
+    s->submitted = s->completed = s->failed = s->batches = s->batched = s->rejected = 0;
     s->t_first = -1;
     s->t_last = 0;
     s->bytes_peak = s->bytes_in_use;

@@ -7,7 +7,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import Request, Result, ServerConfig, ServerStats, lib
+from ._lib import REQUEST_DTYPE, RESULT_DTYPE, Request, Result, ServerConfig, ServerStats, lib
 from .api import _check
 
 REQ_LU, REQ_CHOLESKY, REQ_LSTSQ, REQ_RESOLVE = 0, 1, 2, 3
@@ -19,8 +19,9 @@ def _vp(a: np.ndarray) -> int:
 
 
 class Server:
-    def __init__(self, hbm_budget_bytes: int = 0, workers: int = 0, max_batch: int = 0, small_n: int = 0):
-        cfg = ServerConfig(hbm_budget_bytes, workers, max_batch, small_n)
+    def __init__(self, hbm_budget_bytes: int = 0, workers: int = 0, max_batch: int = 0, small_n: int = 0,
+                 max_pending: int = 0):
+        cfg = ServerConfig(hbm_budget_bytes, workers, max_batch, small_n, max_pending)
         h = C.c_void_p()
         _check(lib.rl_server_create(C.byref(cfg), C.byref(h)))
         self._h = h
@@ -86,6 +87,18 @@ class Server:
         _check(lib.rl_server_replay(self._h, count, arr.ctypes.data_as(C.c_void_p), reqs, res))
         return [{"status": r.status, "iters": r.iters, "path": PATHS.get(r.path, r.path), "berr": r.berr,
                  "latency_us": r.latency_us, "queue_us": r.queue_us, "x": xs[i]} for i, r in enumerate(res)]
+
+    def replay_arrays(self, arrivals_s, requests: np.ndarray) -> np.ndarray:
+        """A request stream as a numpy array of REQUEST_DTYPE records (host pointers in the
+        a / b / x fields; the caller keeps those buffers alive), submitted at arrivals_s by
+        the library's replay thread. Returns a RESULT_DTYPE array (status RL_ERR_BUSY = 37
+        for requests refused by backpressure)."""
+        reqs = np.ascontiguousarray(requests, dtype=REQUEST_DTYPE)
+        arr = np.ascontiguousarray(arrivals_s, dtype=np.float64)
+        res = np.zeros(len(reqs), dtype=RESULT_DTYPE)
+        _check(lib.rl_server_replay(self._h, len(reqs), arr.ctypes.data_as(C.c_void_p),
+                                    reqs.ctypes.data_as(C.c_void_p), res.ctypes.data_as(C.c_void_p)))
+        return res
 
     def close(self) -> None:
         if getattr(self, "_h", None) is not None and self._h.value:
