@@ -50,13 +50,18 @@ def parse():
                    help="CPU baseline sample size in GFLOP of factorisation work")
     p.add_argument("--skip-e2e", action="store_true")
     p.add_argument("--skip-cpu", action="store_true")
-    p.add_argument("--workload", default="batch", choices=["batch", "dense", "mixed", "serve", "peaks"],
-                   help="batch: the headline batched mix (default); dense: GEMM sweep n=1024..8192 f32/f64 "
-                        "and plain FP64 LU; mixed: single-system mixed precision vs FP64 over n and kappa; "
-                        "serve: Poisson request stream through the serving loop; peaks: DFMA / FP64 mma / "
-                        "FFMA / host-copy probes (bench_peaks.cu)")
+    p.add_argument("--workload", default="batch", choices=["batch", "dense", "mixed", "serve"],
+                   help="batch (default): the headline batched mix, followed by the other configurations as "
+                        "sub-objects of the same line; dense / mixed / serve: only that configuration, as its "
+                        "own line (GEMM sweep + FP64 LU; single-system mixed precision; served stream)")
+    p.add_argument("--configs", default="1,2,3,4f,5",
+                   help="configurations reported beside the headline: 1 (LU n=1024), 2 (GEMM sweep, FP64 LU), "
+                        "3 (mixed single systems), 4f (f32 SPD half of the batch), 5 (served stream); '' for none")
     p.add_argument("--sizes", default="", help="comma-separated sizes for dense / mixed")
+    p.add_argument("--kappas", default="1e2,1e6,1e10", help="mixed: condition numbers")
+    p.add_argument("--nrhs", default="1,64", help="mixed: right-hand-side counts")
     p.add_argument("--lambdas", default="1000,10000,50000", help="serve: arrival rates (requests/s)")
+    p.add_argument("--serve-seconds", type=float, default=60.0, help="serve: stream length per rate")
     return p.parse_args()
 
 
@@ -221,227 +226,285 @@ def event_times(fn, steps, warmup, stream, flush=None):
     return out
 
 
-def dense_workload(args, rank, world, dev):
-    """GEMM sweep (f32 / f64, n = 1024 .. 8192) and plain FP64 LU solves: TFLOP/s against
-    the measured FP64 and FP32 peaks, cuBLAS (torch.matmul) beside it for context, and
-    the accuracy bound n eps ||A|| ||B|| (inf-norms) checked against an FP64 product."""
+FP64_PEAK_TFLOPS = 1.25  # GB300's FP64 rate (nominal; rl_dgemm_dev sustains it at n = 8192)
+
+
+def peaks():
+    return json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+
+
+def tf32x3_ceiling_tflops():
+    """FP32-accurate ceiling of the 3xTF32 tensor-core GEMM: the TF32 rate (half the
+    measured bf16 burst rate) over the three TF32 products per FP32 product."""
+    return peaks().get("bf16_tflops", 1900.0) / 2.0 / 3.0
+
+
+def config1(dev):
+    """PartialPivLu decompose + solve, f64, n = 1024, A = U(-1,1) + I (seed 0), b = A x_true:
+    permutation against the oracle, L/U normwise errors, backward and forward errors."""
+    import hashlib
+
+    import torch
+    import oracle as O
+    import rulinalg_gb300 as rl
+    from rulinalg_gb300._lib import SolveInfo
+    import ctypes as C
+    from rulinalg_gb300.workloads import config1_lu
+    n = 1024
+    a, x_true, b = config1_lu(n, seed=0)
+    olu, operm, st, gap = O.lu_decompose(a, gaps=True)
+    t0 = time.perf_counter()
+    lu = rl.PartialPivLu.decompose(a)
+    x = lu.solve(b)
+    host_ms = 1e3 * (time.perf_counter() - t0)
+    lref, uref = np.tril(olu, -1), np.triu(olu)
+    fro = lambda m: float(np.sqrt(np.sum(m * m)))
+    xo, _ = O.lu_solve(olu, operm, b)
+    r = b - a @ x
+    berr = float(np.max(np.abs(r)) / (np.max(np.sum(np.abs(a), 1)) * np.max(np.abs(x)) + np.max(np.abs(b))))
+    stream = torch.cuda.current_stream()
+    ta, tb = torch.from_numpy(a).to(dev), torch.from_numpy(b.reshape(n, 1)).to(dev)
+    tx = torch.zeros_like(tb)
+    info = SolveInfo()
+    call = lambda: rl.lib.rl_dsolve_fp64_dev(n, 1, 0, ta.data_ptr(), n, tb.data_ptr(), 1, tx.data_ptr(), 1,
+                                             C.byref(info), stream.cuda_stream)
+    ms = statistics.median(event_times(call, 5, 3, stream))
+    return {"workload": "PartialPivLu decompose + solve, f64, n=1024, U(-1,1)+I seed 0, b = A x_true",
+            "perm_bit_identical_to_oracle": bool(np.array_equal(lu.p.perm, operm)),
+            "perm_sha256": hashlib.sha256(lu.p.perm.astype("<u8").tobytes()).hexdigest()[:16],
+            "min_pivot_gap": float(gap[:-1].min()),
+            "l_rel_err_vs_oracle": fro(np.tril(lu.lu, -1) - lref) / fro(lref),
+            "u_rel_err_vs_oracle": fro(np.triu(lu.lu) - uref) / fro(uref),
+            "berr": berr, "berr_within": berr <= n * U64 * 10,
+            "fwd_err_vs_oracle": float(np.max(np.abs(x - xo)) / np.max(np.abs(xo))),
+            "fwd_err_vs_x_true": float(np.max(np.abs(x - x_true)) / np.max(np.abs(x_true))),
+            "device_ms": ms, "host_api_ms": host_ms,
+            "tflops": (2.0 * n ** 3 / 3.0 + 2.0 * n * n) / (ms / 1e3) / 1e12}
+
+
+def config2(dev, sizes=(1024, 2048, 4096, 8192), steps=3, warm=3):
+    """Square GEMM sweep (N(0,1), seeded), f32 and f64, and the plain FP64 LU solve at the
+    largest size: TFLOP/s, fraction of the FP64 rate / the 3xTF32 ceiling, cuBLAS beside
+    it for context, and the normwise accuracy bound n eps ||A||_F ||B||_F against an FP64
+    product."""
     import torch
     import rulinalg_gb300 as rl
     from rulinalg_gb300.workloads import config1_lu
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
-    sizes = [int(x) for x in args.sizes.split(",")] if args.sizes else [1024, 2048, 4096, 8192]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    steps, warm = max(1, args.steps), max(3, args.warmup)
+    ceil32 = tf32x3_ceiling_tflops()
     sweep = []
-    l0 = rl.launch_count()
-    with ClockSampler(dev.index or 0) as clk:
-        for n in sizes:
-            g = torch.Generator(device=dev)
-            g.manual_seed(n)
-            a64 = torch.randn(n, n, dtype=torch.float64, device=dev, generator=g)
-            b64 = torch.randn(n, n, dtype=torch.float64, device=dev, generator=g)
-            ref = a64 @ b64
-            bound_base = float(a64.abs().sum(1).max() * b64.abs().sum(1).max())
-            for dt, fn_name, eps in ((torch.float32, "rl_sgemm_dev", 2.0 ** -24), (torch.float64, "rl_dgemm_dev", U64)):
-                a, b = a64.to(dt), b64.to(dt)
-                c = torch.empty(n, n, dtype=dt, device=dev)
-                f = getattr(rl.lib, fn_name)
-                call = lambda: f(n, n, n, a.data_ptr(), n, b.data_ptr(), n, c.data_ptr(), n, sh)
-                ms = event_times(call, steps, warm, stream, flush)
-                err = float((c.double() - (a.double() @ b.double())).abs().max())
-                cub = event_times(lambda: torch.matmul(a, b, out=c), steps, warm, stream, flush)
-                t = statistics.median(ms) / 1e3
-                sweep.append({"op": "gemm", "n": n, "dtype": "f32" if dt == torch.float32 else "f64",
-                              "ms": statistics.median(ms), "tflops": 2.0 * n ** 3 / t / 1e12,
-                              "cublas_tflops": 2.0 * n ** 3 / (statistics.median(cub) / 1e3) / 1e12,
-                              "max_abs_err": err, "bound": n * eps * bound_base,
-                              "within": err <= n * eps * bound_base})
-            del a64, b64, ref
-        # plain FP64 LU factor + solve (PartialPivLu in FP64, one right-hand side)
-        for n in ([1024] + [s for s in sizes if s >= 4096]):
-            a_h, x_true, b_h = config1_lu(n, seed=0)
-            a = torch.from_numpy(a_h).to(dev)
-            b = torch.from_numpy(b_h).to(dev).reshape(n, 1)
-            x = torch.empty_like(b)
-            call = lambda: rl.lib.rl_dsolve_fp64_dev(n, 1, 0, a.data_ptr(), n, b.data_ptr(), 1, x.data_ptr(), 1,
-                                                     None, sh)
-            ms = event_times(call, max(1, steps // 2), 1, stream, flush)
-            t = statistics.median(ms) / 1e3
-            r = (b - a @ x).abs().max().item()
-            berr = r / (a.abs().sum(1).max().item() * x.abs().max().item() + b.abs().max().item())
-            sweep.append({"op": "lu_fp64_solve", "n": n, "dtype": "f64", "ms": statistics.median(ms),
-                          "tflops": (2.0 * n ** 3 / 3.0 + 2.0 * n * n) / t / 1e12, "berr": berr,
-                          "within": berr <= n * U64 * 10, "x_err": float(np.abs(x.cpu().numpy()[:, 0] - x_true).max())})
-    launches = rl.launch_count() - l0
-    head = next((r for r in sweep if r["op"] == "gemm" and r["dtype"] == "f64" and r["n"] == max(sizes)), sweep[0])
-    fp64_peak = 1.05
-    line = {
-        "metric": f"FP64 GEMM TFLOP/s (n={head['n']})", "value": head["tflops"], "unit": "TFLOP/s", "n_gpus": world,
-        "steps": steps, "warmup": warm, "ms_per_step": head["ms"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "square GEMM sweep f32/f64 + plain FP64 LU solve", "sizes": sizes,
-                   "l2": "256 MB buffer overwritten before every timed call"},
-        "roofline": {"bound": "fp64 pipe", "achieved": head["tflops"], "peak": fp64_peak, "unit": "TFLOP/s",
-                     "frac": head["tflops"] / fp64_peak, "traffic": None,
-                     "peak_source": "FP64 DMMA/DFMA probe on this GB300 (MEASURED_PEAKS.json holds no FP64 figure)"},
-        "sweep": sweep, "gpu_launches": launches, "clocks": clk.summary(),
-    }
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    for n in sizes:
+        g = torch.Generator(device=dev)
+        g.manual_seed(n)
+        a64 = torch.randn(n, n, dtype=torch.float64, device=dev, generator=g)
+        b64 = torch.randn(n, n, dtype=torch.float64, device=dev, generator=g)
+        for dt, fn_name, eps in ((torch.float32, "rl_sgemm_dev", 2.0 ** -24), (torch.float64, "rl_dgemm_dev", U64)):
+            a, b = a64.to(dt), b64.to(dt)
+            c = torch.empty(n, n, dtype=dt, device=dev)
+            f = getattr(rl.lib, fn_name)
+            call = lambda: f(n, n, n, a.data_ptr(), n, b.data_ptr(), n, c.data_ptr(), n, sh)
+            ms = statistics.median(event_times(call, steps, warm, stream, flush))
+            ref = a.double() @ b.double()
+            err = float(torch.linalg.norm(c.double() - ref))
+            bound = n * eps * float(torch.linalg.norm(a.double())) * float(torch.linalg.norm(b.double()))
+            cub = statistics.median(event_times(lambda: torch.matmul(a, b, out=c), steps, warm, stream, flush))
+            tf = 2.0 * n ** 3 / (ms / 1e3) / 1e12
+            peak = FP64_PEAK_TFLOPS if dt == torch.float64 else ceil32
+            sweep.append({"n": n, "dtype": "f64" if dt == torch.float64 else "f32", "ms": ms, "tflops": tf,
+                          "frac": tf / peak, "peak_tflops": peak, "cublas_tflops": 2.0 * n ** 3 / (cub / 1e3) / 1e12,
+                          "err_over_bound": err / bound, "within": err <= bound})
+            del ref
+        del a64, b64
+    n = max(sizes)
+    a_h, x_true, b_h = config1_lu(n, seed=0)
+    a = torch.from_numpy(a_h).to(dev)
+    b = torch.from_numpy(b_h).to(dev).reshape(n, 1)
+    x = torch.empty_like(b)
+    call = lambda: rl.lib.rl_dsolve_fp64_dev(n, 1, 0, a.data_ptr(), n, b.data_ptr(), 1, x.data_ptr(), 1, None, sh)
+    ms = statistics.median(event_times(call, 2, 1, stream, flush))
+    r = (b - a @ x).abs().max().item()
+    berr = r / (a.abs().sum(1).max().item() * x.abs().max().item() + b.abs().max().item())
+    tf = (2.0 * n ** 3 / 3.0 + 2.0 * n * n) / (ms / 1e3) / 1e12
+    return {"workload": "square GEMM C = A B, N(0,1), f32 (tcgen05 3xTF32) and f64 (DFMA); plain FP64 LU solve",
+            "peaks": {"f64_tflops": FP64_PEAK_TFLOPS, "f64_source": "GB300 FP64 rate (nominal)",
+                      "f32_tflops": ceil32, "f32_source": "MEASURED_PEAKS bf16 burst / 2 (TF32) / 3 (3xTF32), of measured"},
+            "gemm": sweep,
+            "fp64_lu_solve": {"n": n, "ms": ms, "tflops": tf, "frac_of_fp64_rate": tf / FP64_PEAK_TFLOPS,
+                              "berr": berr, "within": berr <= n * U64 * 10},
+            "l2": "256 MB buffer overwritten before every timed call"}
 
 
-def mixed_workload(args, rank, world, dev):
-    """Single large systems: mixed-precision solve (FP32 factor, FP64 refinement,
-    GMRES-IR, FP64 refactor) against the plain FP64 GPU solve, A = U diag(sigma) V^T with
-    Haar U, V and geometric sigma (condition number kappa), nrhs N(0,1) columns."""
+def config3(dev, sizes=(4096, 8192, 16384), kappas=(1e2, 1e6, 1e10), nrhs_list=(1, 64)):
+    """Mixed-precision single-system LU solves (FP32 factor, FP64 refinement, GMRES-IR,
+    FP64 refactor) against the plain FP64 GPU solve: A = U diag(sigma) V^T, Haar U, V,
+    sigma geometric from 1 to 1/kappa, 1 and 64 N(0,1) right-hand sides. Forward error of
+    the mixed solution against the plain FP64 GPU solution (all sizes) and against the
+    FP64 oracle (n = 4096, elimination rows over all host threads)."""
     import torch
+    import ctypes as C
     import rulinalg_gb300 as rl
     from rulinalg_gb300._lib import SolveInfo
-    import ctypes as C
     from rulinalg_gb300.workloads import conditioned_system
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
-    sizes = [int(x) for x in args.sizes.split(",")] if args.sizes else [4096, 8192, 16384]
-    kappas = [1e2, 1e6, 1e10]
-    cases = []
-    l0 = rl.launch_count()
     paths = {0: "refinement", 1: "gmres-ir", 2: "fp64"}
-    with ClockSampler(dev.index or 0) as clk:
-        for n in sizes:
-            reps = 3 if n <= 8192 else 1
-            for kappa in kappas:
-                a, bfull = conditioned_system(n, kappa, 64, seed=n, device=dev)
-                for nrhs in (1, 64):
-                    b = bfull[:, :nrhs].contiguous()
+    cases = []
+    for n in sizes:
+        reps = 3 if n <= 8192 else 1
+        for kappa in kappas:
+            a, bfull = conditioned_system(n, kappa, 64, seed=n + int(np.log10(kappa)), device=dev)
+            xo_all = None
+            if n == 4096 and 64 in nrhs_list:
+                import oracle as O
+                ah, bh = a.cpu().numpy(), bfull.cpu().numpy()
+                lu, perm, st = O.lu_decompose(ah, threads=os.cpu_count() or 1)
+                xo_all, _ = O.solve_columns(lu, perm, bh, threads=os.cpu_count() or 1)
+            for nrhs in nrhs_list:
+                b = bfull[:, :nrhs].contiguous()
+                row = {"n": n, "kappa": kappa, "nrhs": nrhs}
+                xs = {}
+                for name, fn in (("mixed", rl.lib.rl_dsolve_mixed_dev), ("fp64", rl.lib.rl_dsolve_fp64_dev)):
                     x = torch.empty_like(b)
-                    row = {"n": n, "kappa": kappa, "nrhs": nrhs}
-                    for name, fn in (("mixed", rl.lib.rl_dsolve_mixed_dev), ("fp64", rl.lib.rl_dsolve_fp64_dev)):
-                        info = SolveInfo()
-                        call = lambda: fn(n, nrhs, 0, a.data_ptr(), n, b.data_ptr(), nrhs, x.data_ptr(), nrhs,
-                                          C.byref(info), sh)
-                        ms = event_times(call, reps, 1, stream)
-                        row[name] = {"ms": statistics.median(ms), "berr": info.berr, "iters": info.iters,
-                                     "gmres_iters": info.gmres_iters, "path": paths.get(info.path, info.path),
-                                     "within": info.berr <= n * U64 * 10}
-                    row["speedup"] = row["fp64"]["ms"] / row["mixed"]["ms"]
-                    cases.append(row)
-                del a, bfull
-    launches = rl.launch_count() - l0
+                    info = SolveInfo()
+                    call = lambda: fn(n, nrhs, 0, a.data_ptr(), n, b.data_ptr(), nrhs, x.data_ptr(), nrhs,
+                                      C.byref(info), sh)
+                    ms = statistics.median(event_times(call, reps, 1, stream))
+                    row[name] = {"ms": ms, "berr": info.berr, "iters": info.iters, "gmres_iters": info.gmres_iters,
+                                 "path": paths.get(info.path, info.path), "within": info.berr <= n * U64 * 10}
+                    xs[name] = x
+                fe = torch.linalg.norm(xs["mixed"] - xs["fp64"], dim=0) / torch.linalg.norm(xs["fp64"], dim=0)
+                row["mixed"]["fwd_err_vs_fp64_gpu"] = float(fe.max())
+                if xo_all is not None:
+                    xo = torch.from_numpy(np.ascontiguousarray(xo_all[:, :nrhs])).to(dev)
+                    fo = torch.linalg.norm(xs["mixed"] - xo, dim=0) / torch.linalg.norm(xo, dim=0)
+                    row["mixed"]["fwd_err_vs_oracle"] = float(fo.max())
+                row["speedup"] = row["fp64"]["ms"] / row["mixed"]["ms"]
+                cases.append(row)
+            del a, bfull
     sp = [c["speedup"] for c in cases]
-    geo = float(np.exp(np.mean(np.log(sp))))
-    line = {
-        "metric": "mixed-precision / plain FP64 single-system solve speedup at equal backward error (geomean)",
-        "value": geo, "unit": "x", "n_gpus": world, "steps": 1, "warmup": 1,
-        "ms_per_step": float(np.mean([c["mixed"]["ms"] for c in cases])), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32 factor + f64 refinement", "data": "synthetic",
-        "config": {"workload": "A = U diag(sigma) V^T, Haar U, V", "sizes": sizes, "kappas": kappas, "nrhs": [1, 64],
-                   "l2": "inputs 128 MB+ per matrix > L2"},
-        "cases": cases, "all_within": all(c["mixed"]["within"] for c in cases),
-        "gpu_launches": launches, "clocks": clk.summary(),
-    }
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    return {"workload": "A = U diag(sigma) V^T (Haar U, V; sigma geometric 1 .. 1/kappa), nrhs N(0,1)",
+            "geomean_speedup_mixed_over_fp64": float(np.exp(np.mean(np.log(sp)))),
+            "all_within": all(c["mixed"]["within"] for c in cases), "cases": cases}
 
 
-def serve_workload(args, rank, world, dev):
-    """A Poisson request stream through the serving loop: sizes log-uniform in [16, 4096];
-    70% fresh systems (50% LU, 30% Cholesky, 20% QR least squares with m = 2n) and 30%
-    re-solves against resident LU factors. Systems come from a seeded pool that the
-    requests cycle through (the host arrays are read-only; each request has its own x)."""
+def config4_f32(dev, args):
+    """The f32 half of the SPD set: 20,000 Cholesky systems as Matrix<f32> (FP32 plan,
+    graph-captured, device pointers)."""
+    import torch
     import rulinalg_gb300 as rl
-    from rulinalg_gb300.workloads import log_uniform_sizes
+    n, kind, a, b = workloads_module().mixed_batch(args.count_spd, 0, seed=args.seed, device=dev, dtype=np.float32)
+    count = len(n)
+    stream = torch.cuda.current_stream()
+    plan = rl.BatchPlan(n, kind, rl.PREC_FP32)
+    x = torch.zeros_like(b)
+    info = torch.zeros(count, dtype=torch.int32, device=dev)
+    berr = torch.zeros(count, dtype=torch.float64, device=dev)
+    call = lambda: plan.solve_dev(a.data_ptr(), b.data_ptr(), x.data_ptr(), info.data_ptr(), 0, berr.data_ptr(),
+                                  stream.cuda_stream)
+    ms = statistics.mean(event_times(call, max(3, args.steps), max(3, args.warmup), stream))
+    plan.close()
+    limit = torch.from_numpy(n.astype(np.float64) * 2.0 ** -24 * 10).to(dev)
+    return {"workload": f"{count} SPD systems A = G G^T + n I in f32 (Cholesky, FP32 plan)",
+            "solves_per_s": count / (ms / 1e3), "ms_per_step": ms, "all_ok": bool((info == 0).all()),
+            "max_berr": float(berr.max()), "berr_within_n_u32_10": bool((berr <= limit).all())}
+
+
+def config5(dev, args):
+    """The served stream: Poisson arrivals at each lambda for args.serve_seconds s, sizes
+    log-uniform in [16, 4096], kinds 50% LU / 30% Cholesky / 20% QR least squares (m = 2n,
+    N(0,1)), 30% of requests re-solving a resident LU factor with a new right-hand side.
+    Matrices come from a seeded pool that the requests cycle through (read-only host
+    arrays); results land in per-entry output slots (their values are not read: every
+    result's f64 accuracy is the backward error the server reports). Admission by HBM
+    footprint; backpressure: at most max_pending requests in the server, the rest refused
+    (RL_ERR_BUSY) and counted."""
+    import rulinalg_gb300 as rl
+    from rulinalg_gb300._lib import REQUEST_DTYPE
+    wl = workloads_module()
     rng = np.random.default_rng(args.seed)
-    pool = {0: [], 1: [], 2: []}
     per_kind = 24
+    pool = {0: [], 1: [], 2: []}
     for kind in (0, 1, 2):
-        for n in log_uniform_sizes(per_kind, 16, 4096, rng):
-            n = int(n)
+        for nn in wl.log_uniform_sizes(per_kind, 16, 4096, rng):
+            nn = int(nn)
             if kind == 0:
-                a = rng.uniform(-1, 1, (n, n)) + n * np.eye(n)
+                a = rng.uniform(-1, 1, (nn, nn)) + nn * np.eye(nn)
             elif kind == 1:
-                u = rng.uniform(-1, 1, (n, n))
-                a = 0.5 * (u + u.T) + n * np.eye(n)
+                u = rng.uniform(-1, 1, (nn, nn))
+                a = 0.5 * (u + u.T) + nn * np.eye(nn)
             else:
-                a = rng.standard_normal((2 * n, n))
-            pool[kind].append((a, rng.standard_normal(a.shape[0])))
-    srv = rl.Server()
+                a = rng.standard_normal((2 * nn, nn))
+            pool[kind].append((np.ascontiguousarray(a), rng.standard_normal(a.shape[0]),
+                               [np.zeros(nn) for _ in range(4)]))
+    max_pending = 2048
+    srv = rl.Server(max_pending=max_pending)
     resident = []
-    for n in log_uniform_sizes(8, 16, 4096, rng):
-        n = int(n)
-        a = rng.uniform(-1, 1, (n, n)) + n * np.eye(n)
-        t, _ = srv.submit(rl.REQ_LU, a, rng.standard_normal(n), retain=True)
-        r = srv.wait(t)
-        resident.append((r["factor"], n))
-    lambdas = [float(x) for x in args.lambdas.split(",")]
+    for nn in wl.log_uniform_sizes(8, 16, 4096, rng):
+        nn = int(nn)
+        a = rng.uniform(-1, 1, (nn, nn)) + nn * np.eye(nn)
+        t, _ = srv.submit(rl.REQ_LU, a, rng.standard_normal(nn), retain=True)
+        resident.append((srv.wait(t)["factor"], nn, rng.standard_normal(nn), [np.zeros(nn) for _ in range(4)]))
+    names = {0: "lu", 1: "cholesky", 2: "lstsq", 3: "resolve"}
     runs = []
-    with ClockSampler(dev.index or 0) as clk:
-        for lam in lambdas:
-            count = int(min(4000, max(1000, lam * 0.5)))
-            arrivals = np.cumsum(rng.exponential(1.0 / lam, count))
-            reqs = []
-            for i in range(count):
-                if rng.random() < 0.3:
-                    h, n = resident[int(rng.integers(len(resident)))]
-                    reqs.append((rl.REQ_RESOLVE, None, rng.standard_normal(n), h))
-                else:
-                    kind = int(rng.choice(3, p=[0.5, 0.3, 0.2]))
-                    a, b = pool[kind][int(rng.integers(per_kind))]
-                    reqs.append(({0: rl.REQ_LU, 1: rl.REQ_CHOLESKY, 2: rl.REQ_LSTSQ}[kind], a, b, 0))
-            srv.reset_stats()
-            t0 = time.perf_counter()
-            res = srv.replay(arrivals, reqs)
-            wall = time.perf_counter() - t0
-            st = srv.stats()
-            ok = sum(1 for r in res if r["status"] == 0)
-            berrs = [r["berr"] for r, q in zip(res, reqs) if q[0] != rl.REQ_LSTSQ]
-            by_kind = {}
-            names = {rl.REQ_LU: "lu", rl.REQ_CHOLESKY: "cholesky", rl.REQ_LSTSQ: "lstsq", rl.REQ_RESOLVE: "resolve"}
-            for k, nm in names.items():
-                lat = sorted(r["latency_us"] / 1e3 for r, q in zip(res, reqs) if q[0] == k)
-                if lat:
-                    by_kind[nm] = {"count": len(lat), "p50_ms": lat[len(lat) // 2],
-                                   "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))]}
-            runs.append({"lambda": lam, "requests": count, "ok": ok, "by_kind": by_kind, "p50_ms": st["p50_us"] / 1e3,
-                         "p99_ms": st["p99_us"] / 1e3, "mean_ms": st["mean_us"] / 1e3,
-                         "solves_per_s": st["solves_per_s"], "wall_s": wall, "batches": st["batches"],
-                         "batched_requests": st["batched_requests"], "bytes_peak": st["bytes_peak"],
-                         "max_berr": max(berrs) if berrs else None})
+    for lam in [float(v) for v in args.lambdas.split(",")]:
+        count = int(lam * args.serve_seconds)
+        arrivals = np.cumsum(rng.exponential(1.0 / lam, count))
+        req = np.zeros(count, dtype=REQUEST_DTYPE)
+        is_res = rng.random(count) < 0.3
+        kinds = rng.choice(3, size=count, p=[0.5, 0.3, 0.2])
+        which = rng.integers(0, per_kind, count)
+        rwhich = rng.integers(0, len(resident), count)
+        slot = np.arange(count) % 4
+        kind_of = np.where(is_res, 3, kinds)
+        req["kind"] = kind_of
+        for k in (0, 1, 2):
+            for e in range(per_kind):
+                sel = (~is_res) & (kinds == k) & (which == e)
+                if not sel.any():
+                    continue
+                a, b, xs = pool[k][e]
+                req["m"][sel] = a.shape[0]
+                req["n"][sel] = a.shape[1]
+                req["a"][sel] = a.ctypes.data
+                req["b"][sel] = b.ctypes.data
+                req["x"][sel] = np.array([x.ctypes.data for x in xs], dtype=np.uint64)[slot[sel]]
+        for e, (h, nn, b, xs) in enumerate(resident):
+            sel = is_res & (rwhich == e)
+            req["factor"][sel] = h
+            req["m"][sel] = nn
+            req["n"][sel] = nn
+            req["b"][sel] = b.ctypes.data
+            req["x"][sel] = np.array([x.ctypes.data for x in xs], dtype=np.uint64)[slot[sel]]
+        srv.reset_stats()
+        t0 = time.perf_counter()
+        res = srv.replay_arrays(arrivals, req)
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        ok = res["status"] == 0
+        busy = res["status"] == 37
+        by_kind = {}
+        for k, nm in names.items():
+            sel = ok & (kind_of == k)
+            lat = np.sort(res["latency_us"][sel]) / 1e3
+            if len(lat):
+                by_kind[nm] = {"completed": int(sel.sum()), "p50_ms": float(lat[len(lat) // 2]),
+                               "p99_ms": float(lat[min(len(lat) - 1, int(0.99 * len(lat)))])}
+        sq = ok & (kind_of != 2)
+        lat = np.sort(res["latency_us"][ok]) / 1e3
+        runs.append({"lambda": lam, "seconds": args.serve_seconds, "offered": count, "accepted": int((~busy).sum()),
+                     "rejected_busy": int(busy.sum()), "completed_ok": int(ok.sum()),
+                     "failed": int((~ok & ~busy).sum()), "solves_per_s": float(ok.sum() / wall), "wall_s": wall,
+                     "p50_ms": float(lat[len(lat) // 2]) if len(lat) else None,
+                     "p99_ms": float(lat[min(len(lat) - 1, int(0.99 * len(lat)))]) if len(lat) else None,
+                     "by_kind": by_kind, "batches": st["batches"], "batched_requests": st["batched_requests"],
+                     "bytes_peak": st["bytes_peak"],
+                     "max_berr_lu_chol_resolve": float(res["berr"][sq].max()) if sq.any() else None})
     srv.close()
-    head = runs[0]
-    line = {
-        "metric": f"served solves/s and p99 latency (Poisson, lambda={int(head['lambda'])}/s)",
-        "value": head["solves_per_s"], "unit": "solves/s", "n_gpus": world, "steps": len(runs), "warmup": 0,
-        "ms_per_step": head["p99_ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 factor + f64 refinement (LU/Cholesky), f64 (QR)", "data": "synthetic",
-        "config": {"workload": "served stream: sizes log-uniform [16,4096], 50% LU / 30% Cholesky / 20% QR LS "
-                               "(m=2n), 30% re-solves", "pool_per_kind": per_kind, "resident_factors": len(resident)},
-        "runs": runs, "clocks": clk.summary(),
-    }
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-
-
-def peaks_workload(args, rank, world, dev):
-    """Builds and runs bench_peaks.cu (FP64 / FP32 pipe and host-copy probes)."""
-    import re
-    import tempfile
-    exe = Path(tempfile.mkdtemp()) / "bench_peaks"
-    subprocess.run(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
-                    str(ROOT / "bench_peaks.cu"), "-o", str(exe)], check=True)
-    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
-    vals = {}
-    for key, pat in (("dfma_tflops", r"DFMA\s+\S+ ms\s+(\S+) TFLOP"), ("ffma_tflops", r"FFMA\s+\S+ ms\s+(\S+) TFLOP"),
-                     ("dmma_m8n8k4_tflops", r"DMMA884\s+\S+ ms\s+(\S+) TFLOP"),
-                     ("dmma_m16n8k16_tflops", r"DMMA16816\s+\S+ ms\s+(\S+) TFLOP"),
-                     ("h2d_pinned_gbs", r"H2D pinned \S+ \S+ ms (\S+) GB"), ("d2h_pinned_gbs", r"D2H pinned \S+ \S+ ms (\S+) GB"),
-                     ("h2d_pageable_gbs", r"H2D pageable \S+ \S+ ms (\S+) GB")):
-        m = re.search(pat, out)
-        vals[key] = float(m.group(1)) if m else None
-    if rank == 0:
-        print(json.dumps({"metric": "FP64 DFMA peak", "value": vals["dfma_tflops"], "unit": "TFLOP/s", "n_gpus": world,
-                          "steps": 1, "warmup": 1, "higher_is_better": True, "data": "synthetic",
-                          "probes": vals, "raw": out.strip().splitlines()}), flush=True)
+    return {"workload": "Poisson stream, sizes log-uniform [16,4096], 50% LU / 30% Cholesky / 20% QR LS (m=2n), "
+                        "30% re-solves of resident factors",
+            "pool_per_kind": per_kind, "resident_factors": len(resident), "max_pending": max_pending, "runs": runs}
 
 
 def main():
@@ -454,9 +517,6 @@ def main():
     if args.impl == "reference":
         reference_arm(args, rank, world)
         return
-    if args.workload == "peaks":  # needs no library
-        peaks_workload(args, rank, world, None)
-        return
     import torch
     import rulinalg_gb300 as rl
     from rulinalg_gb300.workloads import mixed_batch
@@ -465,9 +525,19 @@ def main():
     torch.cuda.set_device(dev)
     if not rl.device_available():
         raise SystemExit("rulinalg_gb300: no usable sm_103 GPU")
-    other = {"dense": dense_workload, "mixed": mixed_workload, "serve": serve_workload}.get(args.workload)
-    if other is not None:
-        other(args, rank, world, dev)
+    if args.workload != "batch":
+        sizes = tuple(int(v) for v in args.sizes.split(",")) if args.sizes else None
+        with ClockSampler(local) as clk:
+            if args.workload == "dense":
+                out = config2(dev, sizes or (1024, 2048, 4096, 8192))
+            elif args.workload == "mixed":
+                out = config3(dev, sizes or (4096, 8192, 16384), tuple(float(v) for v in args.kappas.split(",")),
+                              tuple(int(v) for v in args.nrhs.split(",")))
+            else:
+                out = config5(dev, args)
+        out["clocks"] = clk.summary()
+        if rank == 0:
+            print(json.dumps({"workload": args.workload, **out}), flush=True)
         if world > 1:
             import torch.distributed as dist
             dist.destroy_process_group()
@@ -575,15 +645,19 @@ def main():
     if prof.exists():
         for line in prof.read_text().splitlines():
             if line.startswith("traffic_per_launch_bytes:"):
-                traffic = float(line.split(":")[1]) * a_bytes / 10.0127e9
-    fp64_peak = 1.25  # TFLOP/s: rl_dgemm_dev sustains this on GB300 (bench.py --workload dense)
+                traffic = float(line.split(":")[1]) * a_bytes / float(line.split("@")[1]) if "@" in line else None
+    fp64_peak = FP64_PEAK_TFLOPS
     fp64_floor_ms = fl64 / (fp64_peak * 1e12) * 1e3
     roofline = {"bound": "hbm", "achieved": alg_bytes / t_k / 1e9, "peak": hbm_peak, "unit": "GB/s",
                 "frac": alg_bytes / t_k / 1e9 / hbm_peak, "traffic": traffic,
                 "traffic_rate_gbs": traffic / t_k / 1e9 if traffic else None,
+                "traffic_source": "not measured in this run: ncu dram__bytes_read+write of one launch of a smaller "
+                                  "batch of the same mix, scaled by matrix bytes (profiles/"
+                                  "batch_solve_kernel_mixed_40k_mix.md)",
                 "kernel": "batch_solve_kernel<double,float,true> (graph: memset + main pass + FP64 fallback pass)",
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6.8 TB/s",
-                "compute": {"fp32_tflops": fl32 / t_k / 1e12, "fp32_peak_tflops_measured": 74.26,
+                "compute": {"fp32_tflops": fl32 / t_k / 1e12, "fp32_simt_peak_tflops": 80.5,
+                            "fp32_peak_source": "152 SMs x 128 FP32 lanes x 2 flops x 2.07 GHz (nominal)",
                             "fp64_tflops": fl64 / t_k / 1e12, "fp64_peak_tflops": fp64_peak,
                             "fp64_floor_ms": fp64_floor_ms, "frac_of_fp64_floor": fp64_floor_ms / ms_mixed,
                             "note": "HBM is not the binding unit (algorithmic bytes are 1/10 of the DRAM "
@@ -601,6 +675,26 @@ def main():
                "sample": f"{len(idx)} of {count} systems, seeded sample ({flops_of(n[idx], kind[idx]) / 1e9:.1f} "
                          f"GFLOP of factorisation), rulinalg-algorithm restatement in C, 1 thread"}
 
+    # forward error of every solution against the FP64 oracle's (all systems, all host threads)
+    if rank == 0 and not args.skip_cpu:
+        import oracle as O
+        a_h = a.cpu().numpy()
+        b_h = b.cpu().numpy()
+        a_off = np.concatenate([[0], np.cumsum(n.astype(np.int64) ** 2)])[:-1]
+        b_off = np.concatenate([[0], np.cumsum(n.astype(np.int64))])[:-1]
+        xo = b_h.copy()
+        t0 = time.perf_counter()
+        oinfo = O.batch_solve(n, kind, a_off, a_h.copy(), b_off, xo, threads=os.cpu_count() or 1)
+        t_or = time.perf_counter() - t0
+        xm = mixed["x"].cpu().numpy()
+        num = np.maximum.reduceat(np.abs(xm - xo), b_off)
+        den = np.maximum.reduceat(np.abs(xo), b_off)
+        fe = num / den
+        acc["fwd_err_vs_oracle"] = {"max": float(fe.max()), "p99": float(np.quantile(fe, 0.99)),
+                                    "oracle_all_ok": bool((oinfo == 0).all()),
+                                    "norm": "||x - x_oracle||_inf / ||x_oracle||_inf per system",
+                                    "oracle_seconds": t_or, "oracle_threads": os.cpu_count() or 1}
+
     lat = sorted(mixed["ms"])
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
@@ -617,6 +711,25 @@ def main():
         "gpu_launches": int(mixed["launches"]),
         "clocks": mixed["clocks"],
     }
+    # the other configurations, each measured on its own (rank 0; replicas would repeat them)
+    wanted = [c for c in args.configs.split(",") if c]
+    if rank == 0 and wanted:
+        del a, b
+        torch.cuda.empty_cache()
+        configs = {}
+        with ClockSampler(local) as clk:
+            for key, name, fn in (("1", "config1_lu_1024", lambda: config1(dev)),
+                                  ("2", "config2_gemm_and_fp64_lu", lambda: config2(dev)),
+                                  ("3", "config3_mixed_single_system", lambda: config3(dev)),
+                                  ("4f", "config4_f32_spd_half", lambda: config4_f32(dev, args)),
+                                  ("5", "config5_served_stream", lambda: config5(dev, args))):
+                if key in wanted:
+                    t0 = time.perf_counter()
+                    configs[name] = fn()
+                    configs[name]["wall_s"] = time.perf_counter() - t0
+                    torch.cuda.empty_cache()
+        configs["clocks"] = clk.summary()
+        line["configs"] = configs
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

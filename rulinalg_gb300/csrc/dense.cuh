@@ -793,14 +793,19 @@ static __global__ void __launch_bounds__(128) trsm_diag_kernel(const T *D, long 
 // between polls (other streams' kernels share the SMs), and every wait is bounded by
 // wait_ns (RL_TUNE_WAIT_TIMEOUT_NS; RL_ERR_TIMEOUT). withhold >= 0 is a test setting
 // (RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK): that block is solved but never published, so the
-// waits for it run out.
+// waits for it run out. With Dinv (the inverses of the operated diagonal blocks, 64 x 64
+// row-major per block, from diag_inverse_kernel) a block's solve is the product
+// x_b = Dinv_b (y_b - folded sums), 16-term dot products over all 256 threads, instead
+// of the 64-step substitution chain: in FP64 that chain's dependent DFMAs cost ~20 us
+// per block on this part.
 // Per-launch state: ctl[0] = ticket, ctl[1 + b] = block b published, zeroed by the host.
 constexpr int kSweepRows = 64, kSweepRhs = 8, kSweepCtas = 32;
-template <class T>
-static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const T *__restrict__ A, long long lda, int n,
+template <class T, class TA = T>
+static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const TA *__restrict__ A, long long lda, int n,
                                                              T *__restrict__ Y, long long ldy, int nrhs, int mode,
                                                              int *ctl, int *status, T tiny,
-                                                             unsigned long long wait_ns, int withhold) {
+                                                             unsigned long long wait_ns, int withhold,
+                                                             const T *__restrict__ Dinv) {
     constexpr int BR = kSweepRows, LDD = BR + 1;
     __shared__ T Ds[BR * LDD];           // the diagonal block
     __shared__ T inv[BR];                 // 1 / d_ii
@@ -817,12 +822,13 @@ static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const T *__restr
         if (s_t >= nb) break;
         const int b = fwd ? s_t : nb - 1 - s_t, r0 = b * BR, bs = min(BR, n - r0);
         // the diagonal block and its reciprocal diagonal: no dependence on other blocks
-        for (int idx = tid; idx < bs * bs; idx += blockDim.x) {
-            const int i = idx / bs, j = idx - i * bs;
-            Ds[i * LDD + j] = A[(long long)(r0 + i) * lda + r0 + j];
-        }
+        if (!Dinv)
+            for (int idx = tid; idx < bs * bs; idx += blockDim.x) {
+                const int i = idx / bs, j = idx - i * bs;
+                Ds[i * LDD + j] = T(A[(long long)(r0 + i) * lda + r0 + j]);
+            }
         __syncthreads();
-        if (tid < bs) {
+        if (tid < bs && !Dinv) {
             const T d = Ds[tid * LDD + tid];
             if (mode != 0 && absT(d) < tiny) atomicCAS(status, 0, RL_ERR_DIV_BY_ZERO);
             inv[tid] = mode == 0 ? T(1) : T(1) / d;
@@ -841,7 +847,7 @@ static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const T *__restr
             for (int jj = 0; jj < 16; jj++) {
                 const int j = q * 16 + jj;
                 a[jj] = (r < bs && j < ks)
-                            ? (trans ? A[(long long)(c0 + j) * lda + r0 + r] : A[(long long)(r0 + r) * lda + c0 + j])
+                            ? T(trans ? A[(long long)(c0 + j) * lda + r0 + r] : A[(long long)(r0 + r) * lda + c0 + j])
                             : T(0);
             }
             if (tid == 0 && !s_fail) {
@@ -889,8 +895,36 @@ static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const T *__restr
                 __syncthreads();
             }
         }
+        if (Dinv) {
+            // x_b = Dinv_b v, v = y_b - folded sums (in xs); thread (row rr, quarter qq)
+            for (int idx = tid; idx < bs * nrhs; idx += blockDim.x) {
+                const int i = idx / nrhs, c = idx - i * nrhs;
+                xs[i * kSweepRhs + c] = __ldcg(Y + (long long)(r0 + i) * ldy + c) - xs[i * kSweepRhs + c];
+            }
+            __syncthreads();
+            const int rr = tid >> 2, qq = tid & 3;
+            const T *Db = Dinv + (long long)b * BR * BR + (long long)rr * BR + qq * 16;
+            T xo[kSweepRhs];
+    #pragma unroll
+            for (int c = 0; c < kSweepRhs; c++) xo[c] = T(0);
+    #pragma unroll
+            for (int jj = 0; jj < 16; jj++) {
+                const int j = qq * 16 + jj;
+                const T dv = (rr < bs && j < bs) ? Db[jj] : T(0);
+    #pragma unroll
+                for (int c = 0; c < kSweepRhs; c++)
+                    if (c < nrhs) xo[c] = fma(dv, xs[j * kSweepRhs + c], xo[c]);
+            }
+    #pragma unroll
+            for (int c = 0; c < kSweepRhs; c++) {
+                xo[c] += __shfl_xor_sync(0xffffffffu, xo[c], 1);
+                xo[c] += __shfl_xor_sync(0xffffffffu, xo[c], 2);
+            }
+            if (qq == 0 && rr < bs && !s_fail)
+                for (int c = 0; c < nrhs; c++) __stcg(Y + (long long)(r0 + rr) * ldy + c, xo[c]);
+        }
         // substitution: warp c solves right-hand side c; lane l holds rows l and l + 32
-        if (warp < nrhs && !s_fail) {
+        if (!Dinv && warp < nrhs && !s_fail) {
             const int c = warp;
             T y[2];
     #pragma unroll
@@ -947,6 +981,49 @@ static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const T *__restr
             if (b != withhold) st_release(ctl + 1 + b, 1);
         }
     }
+}
+
+// Dinv_b = op(D_b)^-1 for every 64 x 64 diagonal block D_b of A (n x n, stored as TA),
+// formed in T, one CTA per block: 64 threads, thread j solving op(D_b) x = e_j by
+// substitution (op and the unit diagonal as in trsv_sweep_kernel's modes). Written
+// row-major 64 x 64 per block, zero beyond a partial last block. |d_ii| < tiny records
+// RL_ERR_DIV_BY_ZERO.
+template <class T, class TA>
+static __global__ void __launch_bounds__(64) diag_inverse_kernel(const TA *__restrict__ A, long long lda, int n, int mode,
+                                                             T *__restrict__ Dinv, int *status, T tiny) {
+    constexpr int BR = kSweepRows;
+    __shared__ T M[BR][BR + 1];  // op(D_b)
+    __shared__ T X[BR][BR + 1];  // column j: thread j's solution
+    const int b = blockIdx.x, r0 = b * BR, bs = min(BR, n - r0), j = threadIdx.x;
+    for (int idx = j; idx < BR * BR; idx += blockDim.x) {
+        const int r = idx / BR, c = idx - r * BR;
+        T v = T(0);
+        if (r < bs && c < bs)
+            v = T(mode == 3 ? A[(long long)(r0 + c) * lda + r0 + r] : A[(long long)(r0 + r) * lda + r0 + c]);
+        M[r][c] = v;
+        X[r][c] = T(0);
+    }
+    __syncthreads();
+    const bool unit = mode == 0, lower = mode <= 1;
+    if (j < bs) {
+        if (!unit && absT(M[j][j]) < tiny) atomicCAS(status, 0, RL_ERR_DIV_BY_ZERO);
+        if (lower) {
+            for (int i = j; i < bs; i++) {
+                T v = i == j ? T(1) : T(0);
+                for (int k = j; k < i; k++) v = fma(-M[i][k], X[k][j], v);
+                X[i][j] = unit ? v : v / M[i][i];
+            }
+        } else {
+            for (int i = j; i >= 0; i--) {
+                T v = i == j ? T(1) : T(0);
+                for (int k = i + 1; k <= j; k++) v = fma(-M[i][k], X[k][j], v);
+                X[i][j] = v / M[i][i];
+            }
+        }
+    }
+    __syncthreads();
+    T *out = Dinv + (long long)b * BR * BR;
+    for (int idx = j; idx < BR * BR; idx += blockDim.x) out[idx] = X[idx / BR][idx % BR];
 }
 
 // Row-wise solve X D^T = Y for the rows of Y (m x bs, stride ldy), D lower bs x bs:

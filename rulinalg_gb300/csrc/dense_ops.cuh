@@ -168,8 +168,8 @@ rl_status qr_panel_cluster(T *P, long long lda, int mrows, int kb, T *tau, cudaS
 }
 
 // op(A) Y = Y' in place (triangular solve; modes and paths at the definition below).
-template <class T>
-rl_status tri_solve_dev(const T *A, long long lda, int n, T *Y, long long ldy, int nrhs, int mode, int *dstatus,
+template <class T, class TA = T>
+rl_status tri_solve_dev(const TA *A, long long lda, int n, T *Y, long long ldy, int nrhs, int mode, int *dstatus,
                         cudaStream_t s, T tiny = Eps<T>::value);
 
 // Outer block width of the blocked factorisations. FP32 (the mixed-precision factor and
@@ -408,9 +408,11 @@ rl_status qr_first_k_dev(const T *QR, long long lda, int m, int n, const T *tau,
 
 // Blocked triangular solve op(A) X = Y in place (A n x n, Y n x nrhs).
 // mode 0: unit lower, 1: lower, 2: upper, 3: L^T with L lower. |d_ii| < eps is
-// recorded as RL_ERR_DIV_BY_ZERO in *dstatus.
-template <class T>
-rl_status tri_solve_dev(const T *A, long long lda, int n, T *Y, long long ldy, int nrhs, int mode, int *dstatus,
+// recorded as RL_ERR_DIV_BY_ZERO in *dstatus. A may be stored in a narrower type TA than
+// the arithmetic type T for at most kSweepRhs right-hand sides (an FP32 factor applied in
+// FP64).
+template <class T, class TA>
+rl_status tri_solve_dev(const TA *A, long long lda, int n, T *Y, long long ldy, int nrhs, int mode, int *dstatus,
                         cudaStream_t s, T tiny) {
     if (n <= 0 || nrhs <= 0) return RL_OK;
     constexpr int NB = 64;
@@ -422,10 +424,10 @@ rl_status tri_solve_dev(const T *A, long long lda, int n, T *Y, long long ldy, i
             for (int b0 = 0; b0 < n; b0 += NB) {
                 const int bs = std::min(NB, n - b0), rest = n - b0 - bs;
                 T *Yb = Y + (long long)b0 * ldy;
-                RL_LAUNCH(trsv_diag_kernel<T>, 1, 256, 0, s, A + (long long)b0 * lda + b0, lda, bs, Yb, ldy, nrhs, mode,
+                RL_LAUNCH((trsv_diag_kernel<T, TA>), 1, 256, 0, s, A + (long long)b0 * lda + b0, lda, bs, Yb, ldy, nrhs, mode,
                           dstatus, tiny);
                 if (rest > 0)
-                    RL_LAUNCH(gemv_update_kernel<T>, std::min(gridr, ceil_div(rest, wpb)), 32 * wpb, 0, s,
+                    RL_LAUNCH((gemv_update_kernel<T, TA>), std::min(gridr, ceil_div(rest, wpb)), 32 * wpb, 0, s,
                               A + (long long)(b0 + bs) * lda + b0, lda, rest, bs, Yb, ldy, Yb + (long long)bs * ldy,
                               nrhs, false);
             }
@@ -433,14 +435,14 @@ rl_status tri_solve_dev(const T *A, long long lda, int n, T *Y, long long ldy, i
             for (int b1 = n; b1 > 0; b1 -= NB) {
                 const int b0 = std::max(0, b1 - NB), bs = b1 - b0;
                 T *Yb = Y + (long long)b0 * ldy;
-                RL_LAUNCH(trsv_diag_kernel<T>, 1, 256, 0, s, A + (long long)b0 * lda + b0, lda, bs, Yb, ldy, nrhs, mode,
+                RL_LAUNCH((trsv_diag_kernel<T, TA>), 1, 256, 0, s, A + (long long)b0 * lda + b0, lda, bs, Yb, ldy, nrhs, mode,
                           dstatus, tiny);
                 if (b0 > 0) {
                     if (mode == 2)
-                        RL_LAUNCH(gemv_update_kernel<T>, std::min(gridr, ceil_div(b0, wpb)), 32 * wpb, 0, s, A + b0, lda,
+                        RL_LAUNCH((gemv_update_kernel<T, TA>), std::min(gridr, ceil_div(b0, wpb)), 32 * wpb, 0, s, A + b0, lda,
                                   b0, bs, Yb, ldy, Y, nrhs, false);
                     else
-                        RL_LAUNCH(gemv_update_kernel<T>, ceil_div(b0, 256), 256, 0, s, A + (long long)b0 * lda, lda, b0,
+                        RL_LAUNCH((gemv_update_kernel<T, TA>), ceil_div(b0, 256), 256, 0, s, A + (long long)b0 * lda, lda, b0,
                                   bs, Yb, ldy, Y, nrhs, true);
                 }
             }
@@ -454,37 +456,68 @@ rl_status tri_solve_dev(const T *A, long long lda, int n, T *Y, long long ldy, i
         DevBuf<int> ctl;
         RL_TRY(ctl.alloc(1 + nb, s));
         RL_TRY_CUDA(cudaMemsetAsync(ctl.p, 0, sizeof(int) * (1 + nb), s));
-        RL_LAUNCH(trsv_sweep_kernel<T>, std::min(nb, kSweepCtas), 256, 0, s, A, lda, n, Y, ldy, nrhs, mode, ctl.p, dstatus,
-                  tiny, wait_ns(), (int)tune(RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK));
+        RL_LAUNCH((trsv_sweep_kernel<T, TA>), std::min(nb, kSweepCtas), 256, 0, s, A, lda, n, Y, ldy, nrhs, mode, ctl.p, dstatus,
+                  tiny, wait_ns(), (int)tune(RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK), (const T *)nullptr);
         return RL_OK;
     }
-    const int gr = ceil_div(nrhs, kTrsmCols);
-    if (mode == 0 || mode == 1) {
-        for (int b0 = 0; b0 < n; b0 += NB) {
-            const int bs = std::min(NB, n - b0);
-            const T *D = A + (long long)b0 * lda + b0;
-            T *Yb = Y + (long long)b0 * ldy;
-            RL_LAUNCH(trsm_diag_kernel<T>, gr, 128, 0, s, D, lda, bs, Yb, ldy, nrhs, mode, dstatus, tiny);
-            const int rest = n - b0 - bs;
-            if (rest > 0)
-                RL_TRY((gemm<T, false, false>(rest, nrhs, bs, T(-1), A + (long long)(b0 + bs) * lda + b0, lda, Yb, ldy,
-                                              T(1), Yb + (long long)bs * ldy, ldy, s)));
-        }
+    if constexpr (!std::is_same<T, TA>::value) {
+        return RL_ERR_INVALID_ARG;  // mixed storage: few right-hand sides only
     } else {
-        for (int b1 = n; b1 > 0; b1 -= NB) {
-            const int b0 = std::max(0, b1 - NB), bs = b1 - b0;
-            const T *D = A + (long long)b0 * lda + b0;
-            T *Yb = Y + (long long)b0 * ldy;
-            RL_LAUNCH(trsm_diag_kernel<T>, gr, 128, 0, s, D, lda, bs, Yb, ldy, nrhs, mode, dstatus, tiny);
-            if (b0 > 0) {
-                if (mode == 2)
-                    RL_TRY((gemm<T, false, false>(b0, nrhs, bs, T(-1), A + b0, lda, Yb, ldy, T(1), Y, ldy, s)));
-                else
-                    RL_TRY((gemm<T, true, false>(b0, nrhs, bs, T(-1), A + (long long)b0 * lda, lda, Yb, ldy, T(1), Y,
-                                                 ldy, s)));
+        const int gr = ceil_div(nrhs, kTrsmCols);
+        if (mode == 0 || mode == 1) {
+            for (int b0 = 0; b0 < n; b0 += NB) {
+                const int bs = std::min(NB, n - b0);
+                const T *D = A + (long long)b0 * lda + b0;
+                T *Yb = Y + (long long)b0 * ldy;
+                RL_LAUNCH(trsm_diag_kernel<T>, gr, 128, 0, s, D, lda, bs, Yb, ldy, nrhs, mode, dstatus, tiny);
+                const int rest = n - b0 - bs;
+                if (rest > 0)
+                    RL_TRY((gemm<T, false, false>(rest, nrhs, bs, T(-1), A + (long long)(b0 + bs) * lda + b0, lda, Yb, ldy,
+                                                  T(1), Yb + (long long)bs * ldy, ldy, s)));
+            }
+        } else {
+            for (int b1 = n; b1 > 0; b1 -= NB) {
+                const int b0 = std::max(0, b1 - NB), bs = b1 - b0;
+                const T *D = A + (long long)b0 * lda + b0;
+                T *Yb = Y + (long long)b0 * ldy;
+                RL_LAUNCH(trsm_diag_kernel<T>, gr, 128, 0, s, D, lda, bs, Yb, ldy, nrhs, mode, dstatus, tiny);
+                if (b0 > 0) {
+                    if (mode == 2)
+                        RL_TRY((gemm<T, false, false>(b0, nrhs, bs, T(-1), A + b0, lda, Yb, ldy, T(1), Y, ldy, s)));
+                    else
+                        RL_TRY((gemm<T, true, false>(b0, nrhs, bs, T(-1), A + (long long)b0 * lda, lda, Yb, ldy, T(1), Y,
+                                                     ldy, s)));
+                }
             }
         }
+        return RL_OK;
     }
+}
+
+// Inverses of op(A)'s 64 x 64 diagonal blocks, formed in T (ceil(n / 64) row-major
+// 64 x 64 blocks in Dinv; diag_inverse_kernel).
+template <class T, class TA>
+rl_status diag_inverse(const TA *A, long long lda, int n, int mode, T *Dinv, int *dstatus, cudaStream_t s, T tiny) {
+    if (n <= 0) return RL_OK;
+    RL_LAUNCH((diag_inverse_kernel<T, TA>), ceil_div(n, kSweepRows), 64, 0, s, A, lda, n, mode, Dinv, dstatus, tiny);
+    return RL_OK;
+}
+
+// op(A) Y = Y' for at most kSweepRhs right-hand sides in one sweep launch whose block
+// solves are products with the diagonal blocks' inverses Dinv (diag_inverse). More
+// right-hand sides, or a GPU shared with other streams of this library (the serving
+// workers, see tri_solve_dev), take tri_solve_dev's substitution paths instead.
+template <class T, class TA>
+rl_status tri_solve_inv_dev(const TA *A, long long lda, int n, const T *Dinv, T *Y, long long ldy, int nrhs, int mode,
+                            int *dstatus, cudaStream_t s, T tiny) {
+    if (nrhs > kSweepRhs || g_shared_gpu) return tri_solve_dev<T, TA>(A, lda, n, Y, ldy, nrhs, mode, dstatus, s, tiny);
+    if (n <= 0 || nrhs <= 0) return RL_OK;
+    const int nb = ceil_div(n, kSweepRows);
+    DevBuf<int> ctl;
+    RL_TRY(ctl.alloc(1 + nb, s));
+    RL_TRY_CUDA(cudaMemsetAsync(ctl.p, 0, sizeof(int) * (1 + nb), s));
+    RL_LAUNCH((trsv_sweep_kernel<T, TA>), std::min(nb, kSweepCtas), 256, 0, s, A, lda, n, Y, ldy, nrhs, mode, ctl.p,
+              dstatus, tiny, wait_ns(), (int)tune(RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK), Dinv);
     return RL_OK;
 }
 

@@ -117,9 +117,11 @@ static __global__ void f32_to_f64_kernel(const float *__restrict__ W, long long 
 // ------------------------------------------------ few-right-hand-side triangular --
 // Diagonal block solve for nrhs <= 8 right-hand sides: one warp per column, the
 // bs x bs block (bs <= 64) staged in shared memory. mode 0: unit lower, 1: lower,
-// 2: upper, 3: D^T with D lower. |d_ii| < tiny records RL_ERR_DIV_BY_ZERO.
-template <class T>
-static __global__ void __launch_bounds__(256) trsv_diag_kernel(const T *__restrict__ D, long long ldd, int bs,
+// 2: upper, 3: D^T with D lower. |d_ii| < tiny records RL_ERR_DIV_BY_ZERO. The block may
+// be stored in a narrower type TA than the arithmetic type T (an FP32 factor applied in
+// FP64 by GMRES-IR's preconditioner).
+template <class T, class TA = T>
+static __global__ void __launch_bounds__(256) trsv_diag_kernel(const TA *__restrict__ D, long long ldd, int bs,
                                                          T *__restrict__ Y, long long ldy, int nrhs, int mode,
                                                          int *status, T tiny) {
     __shared__ T Ds[64][65];
@@ -127,7 +129,7 @@ static __global__ void __launch_bounds__(256) trsv_diag_kernel(const T *__restri
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int idx = threadIdx.x; idx < bs * bs; idx += blockDim.x) {
         const int i = idx / bs, j = idx - i * bs;
-        Ds[i][j] = D[(long long)i * ldd + j];
+        Ds[i][j] = T(D[(long long)i * ldd + j]);
     }
     const int c = w;
     if (c < nrhs)
@@ -164,16 +166,17 @@ static __global__ void __launch_bounds__(256) trsv_diag_kernel(const T *__restri
 
 // Yr[i][c] -= sum_j M[i][j] Yb[j][c] for i < rows, j < bs (<= 64), c < nrhs (<= 8);
 // warp per row. transposed = true uses M[j][i] (M given with row stride ldm from the
-// block's top-left, i.e. the block is bs x rows) and a thread per output row.
-template <class T>
-static __global__ void gemv_update_kernel(const T *__restrict__ M, long long ldm, int rows, int bs, const T *__restrict__ Yb,
+// block's top-left, i.e. the block is bs x rows) and a thread per output row. M may be
+// stored in a narrower type TA than the arithmetic type T.
+template <class T, class TA = T>
+static __global__ void gemv_update_kernel(const TA *__restrict__ M, long long ldm, int rows, int bs, const T *__restrict__ Yb,
                                    long long ldy, T *__restrict__ Yr, int nrhs, bool transposed) {
     if (!transposed) {
         const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
         for (int i = blockIdx.x * wpb + (threadIdx.x >> 5); i < rows; i += gridDim.x * wpb) {
-            const T *row = M + (long long)i * ldm;
-            const T m0 = lane < bs ? row[lane] : T(0);
-            const T m1 = lane + 32 < bs ? row[lane + 32] : T(0);
+            const TA *row = M + (long long)i * ldm;
+            const T m0 = lane < bs ? T(row[lane]) : T(0);
+            const T m1 = lane + 32 < bs ? T(row[lane + 32]) : T(0);
             for (int c = 0; c < nrhs; c++) {
                 T s = T(0);
                 if (lane < bs) s = m0 * Yb[(long long)lane * ldy + c];
@@ -186,7 +189,7 @@ static __global__ void gemv_update_kernel(const T *__restrict__ M, long long ldm
         for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += gridDim.x * blockDim.x) {
             for (int c = 0; c < nrhs; c++) {
                 T s = T(0);
-                for (int j = 0; j < bs; j++) s = fma(M[(long long)j * ldm + i], Yb[(long long)j * ldy + c], s);
+                for (int j = 0; j < bs; j++) s = fma(T(M[(long long)j * ldm + i]), Yb[(long long)j * ldy + c], s);
                 Yr[(long long)i * ldy + c] -= s;
             }
         }

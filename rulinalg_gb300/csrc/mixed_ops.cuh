@@ -4,6 +4,7 @@
 #pragma once
 
 #include <cfloat>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -64,8 +65,9 @@ inline rl_status precond_solve(const float *F, int n, int kind, const int *ipiv,
     return tri_solve_dev<float>(F, n, n, W, ldw, nrhs, 3, dstatus, s, tiny);
 }
 
-// dst = M^-1 src for one FP64 vector (scaled by its inf-norm around the FP32 solve).
-struct Minv {
+// dst = M^-1 src for one FP64 vector with the solves in FP32 (the vector scaled by its
+// inf-norm around them): the semi-normal-equations preconditioner of lstsq_mixed.
+struct Minv32 {
     const float *F;
     int n, kind;
     const int *ipiv;
@@ -84,6 +86,37 @@ struct Minv {
     }
 };
 
+// dst = M^-1 src for one FP64 vector: the FP32 factor's row swaps and triangular solves
+// in FP64 arithmetic, the factor's entries widened as they are read. Applied in the
+// working precision the preconditioner lets GMRES-IR converge where the FP32-applied form
+// stalls (Carson & Higham's analysis assumes it; on kappa = 1e8 systems with geometric
+// singular values, n = 1024, a CPU model of both took 121 against 313 GMRES iterations).
+// The block solves use the FP64 inverses of the two triangles' 64 x 64 diagonal blocks
+// (D1 for L, D2 for U or L^T), formed once by init().
+struct Minv {
+    const float *F;
+    int n, kind;
+    const int *ipiv;
+    int *dstatus;
+    DevBuf<double> D1, D2;
+    int mode1() const { return kind == RL_KIND_LU ? 0 : 1; }
+    int mode2() const { return kind == RL_KIND_LU ? 2 : 3; }
+    rl_status init(cudaStream_t s) {
+        const size_t blocks = (size_t)ceil_div(n, kSweepRows) * kSweepRows * kSweepRows;
+        RL_TRY(D1.alloc(blocks, s));
+        RL_TRY(D2.alloc(blocks, s));
+        RL_TRY((diag_inverse<double, float>(F, n, n, mode1(), D1.p, dstatus, s, FLT_MIN)));
+        return diag_inverse<double, float>(F, n, n, mode2(), D2.p, dstatus, s, FLT_MIN);
+    }
+    rl_status apply(const double *src, double *dst, cudaStream_t s) const {
+        RL_TRY_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        const double tiny = FLT_MIN;
+        if (kind == RL_KIND_LU) RL_TRY(laswp<double>(dst, 1, 1, 0, 0, ipiv, 0, n, s));
+        RL_TRY((tri_solve_inv_dev<double, float>(F, n, n, D1.p, dst, 1, 1, mode1(), dstatus, s, tiny)));
+        return tri_solve_inv_dev<double, float>(F, n, n, D2.p, dst, 1, 1, mode2(), dstatus, s, tiny);
+    }
+};
+
 // Deterministic dot products h[j] = V[j] . w (j < k1) into out (accumulate adds).
 struct Dots {
     double *partial;
@@ -99,11 +132,16 @@ struct Dots {
 // GMRES-IR on one column: x (contiguous, FP64) refined against b until the FP64
 // backward-error test passes. Restarted GMRES(m) in FP64 on M^-1 A d = M^-1 r with
 // CGS2 orthogonalisation; Givens rotations and the small triangular solve on the GPU.
+// It gives up (ok = false) when a restart cycle does not cut the residual tenfold or when
+// the host clock passes `deadline` (seconds, host_seconds()): past that an FP64
+// refactorisation is the cheaper way to the answer.
+inline double host_seconds() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
 inline rl_status gmres_ir(const double *A, long long lda, int n, const Minv &M, const double *b, double *x, double anorm,
-                   double bnorm, SolveOut &out, bool &ok, cudaStream_t s) {
-    // At most two restart cycles, and the second only if the first cut the residual
-    // tenfold: past that an FP64 refactorisation is the cheaper way to the answer.
-    constexpr int m = 48, outer_max = 3;
+                   double bnorm, double deadline, SolveOut &out, bool &ok, cudaStream_t s) {
+    constexpr int m = 64, outer_max = 5;
     const double inner_tol = 1e-8;
     DevBuf<double> V, H, cs, sn, g, y, w, r, t, nrm2, partial;
     DevBuf<unsigned long long> bits;
@@ -175,6 +213,10 @@ inline rl_status gmres_ir(const double *A, long long lda, int n, const Minv &M, 
             out.gmres++;
             k1 = k + 1;
             if (!(res > inner_tol * beta)) break;
+            if (host_seconds() > deadline) return RL_OK;  // over budget: ok stays false
+            // stagnating in the first cycle (a preconditioner too far off, kappa u_32 >> 1):
+            // the refactor is cheaper than the iterations still ahead
+            if (outer == 0 && k + 1 == 32 && res > 1e-3 * beta) return RL_OK;
         }
         RL_LAUNCH(hsolve_kernel, 1, 32, 0, s, H.p, m + 1, k1, g.p, y.p);
         RL_LAUNCH(combine_kernel, gv, 256, 0, s, x, V.p, (long long)n, k1, y.p, n);
@@ -377,7 +419,7 @@ struct MixedFactor {
         RL_TRY_CUDA(cudaMemset2DAsync(X, ldx * sizeof(double), 0, nrhs * sizeof(double), n, s));
         RL_LAUNCH(update_x_kernel, ge, 256, 0, s, X, ldx, W.p, (long long)nrhs, n, nrhs, bn_b, active.p);
         std::vector<unsigned long long> hb(3 * nrhs);
-        bool stalled = false, need_fp64 = false, diverged = false;
+        bool stalled = false, need_fp64 = false;
         for (int it = 0;; it++) {
             RL_TRY(residual_dev(A, lda, n, X, ldx, B, ldb, R.p, nrhs, nrhs, s));
             RL_TRY(colnorm_dev(R.p, nrhs, n, nrhs, rn_b, s));
@@ -401,9 +443,6 @@ struct MixedFactor {
                 near[c] = rn <= 10.0 * n * kU * den;
                 // diverging (a growing residual) or stalling (not halving after two steps)
                 if (!conv[c] && ((it >= 1 && rn > prev[c]) || (it >= 2 && rn > 0.5 * prev[c]))) stalled = true;
-                // the first correction made things worse: the FP32 factor is too far off
-                // (kappa u_32 >> 1) for GMRES-IR to pay off against an FP64 refactor
-                if (!conv[c] && it == 1 && rn > prev[c]) diverged = true;
                 if (!std::isfinite(rn)) stalled = true;
                 prev[c] = rn;
                 all &= conv[c];
@@ -427,19 +466,23 @@ struct MixedFactor {
             bool all_ok = true;
             for (int c = 0; c < nrhs; c++) all_ok &= conv[c] != 0;
             if (all_ok) return RL_OK;
-            need_fp64 = diverged;
         }
         if (!need_fp64) {
-            // GMRES-IR on each remaining column
+            // GMRES-IR on each remaining column, within a budget of the estimated time of
+            // the FP64 refactor it would otherwise save: the panel chain (~3.3 us per column
+            // measured) plus 2/3 n^3 flops for LU, 1/3 n^3 for Cholesky, at the ~1 TFLOP/s
+            // of the FP64 blocked factorisations. A first correction that grew
+            // (kappa u_32 > 1) does not tell a system GMRES-IR converges on (kappa ~ 1e8)
+            // from one it never will (kappa ~ 1e10); the GMRES residual does (gmres_ir).
             out.path = RL_PATH_GMRES;
+            const double fp64_s =
+                3.3e-6 * n + (kind == RL_KIND_LU ? 2.0 / 3.0 : 1.0 / 3.0) * (double)n * n * n / 1.0e12;
+            const double deadline = host_seconds() + fp64_s;
             DevBuf<double> xb, bb;
-            DevBuf<float> w32;
-            DevBuf<unsigned long long> mb;
             RL_TRY(xb.alloc(n, s));
             RL_TRY(bb.alloc(n, s));
-            RL_TRY(w32.alloc(n, s));
-            RL_TRY(mb.alloc(1, s));
-            Minv M{F, n, kind, ipiv, w32.p, mb.p, active.p + nrhs, dstatus.p + 1};
+            Minv M{F, n, kind, ipiv, dstatus.p + 1, {}, {}};
+            RL_TRY(M.init(s));
             for (int c = 0; c < nrhs && !need_fp64; c++) {
                 if (conv[c]) continue;
                 RL_TRY_CUDA(cudaMemcpy2DAsync(xb.p, sizeof(double), X + c, ldx * sizeof(double), sizeof(double), n,
@@ -448,7 +491,7 @@ struct MixedFactor {
                                               cudaMemcpyDeviceToDevice, s));
                 SolveOut o;
                 bool ok = false;
-                RL_TRY(gmres_ir(A, lda, n, M, bb.p, xb.p, anorm, bnorm[c], o, ok, s));
+                RL_TRY(gmres_ir(A, lda, n, M, bb.p, xb.p, anorm, bnorm[c], deadline, o, ok, s));
                 int dst = 0;
                 RL_TRY_CUDA(cudaMemcpyAsync(&dst, dstatus.p + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
                 RL_TRY_CUDA(cudaStreamSynchronize(s));
@@ -552,7 +595,7 @@ inline rl_status lstsq_mixed(const double *A, long long lda, int m, int n, const
     RL_TRY(qr_factor_dev<float>(Q32.p, n, m, n, n, tau32.p, s));
     RL_LAUNCH(upper_to_lower_t_kernel, (int)std::min<long long>(8 * num_sms(), ((long long)n * n + 255) / 256), 256, 0, s,
               Q32.p, (long long)n, n, L.p);
-    Minv M{L.p, n, RL_KIND_CHOLESKY, nullptr, w32.p, bits.p + 2, one.p, dstatus.p};
+    Minv32 M{L.p, n, RL_KIND_CHOLESKY, nullptr, w32.p, bits.p + 2, one.p, dstatus.p};
     GemvT At{partial.p, chunks, rows_per};
     const int gv = std::min(4 * num_sms(), ceil_div(n, 256));
     // x0 = (R^T R)^-1 A^T b
