@@ -581,8 +581,16 @@ def main():
         plan.close()
         return res
 
-    mixed = time_plan(rl.PREC_MIXED, args.steps, args.warmup)
+    # autotuned launch shape and size classes for each plan (rulinalg_gb300/autotune.py),
+    # cached for this run only, so every bench run tunes on its own GPU
+    import tempfile
+    from rulinalg_gb300 import autotune
+    tune_cache = Path(tempfile.mkdtemp()) / "autotune.json"
+    tuned = {}
+    tuned["fp64"] = autotune.tune(n, kind, rl.PREC_FP64, a, b, reps=2, cache=tune_cache)
     fp64 = time_plan(rl.PREC_FP64, max(2, args.steps // 3), 1)
+    tuned["mixed"] = autotune.tune(n, kind, rl.PREC_MIXED, a, b, reps=3, cache=tune_cache)
+    mixed = time_plan(rl.PREC_MIXED, args.steps, args.warmup)
 
     ms_mixed = aggregate_max(sum(mixed["ms"]) / len(mixed["ms"]), world, dev)
     ms_fp64 = aggregate_max(sum(fp64["ms"]) / len(fp64["ms"]), world, dev)
@@ -704,6 +712,8 @@ def main():
         "plain_fp64_gpu": {"value": v_fp64, "unit": "solves/s", "ms_per_step": ms_fp64,
                            "speedup_mixed_over_fp64": value / v_fp64},
         "batch_latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))]},
+        "autotune": {k: {"choice": v["choice"], "tuned_ms": v["ms"], "default_ms": v["default_ms"],
+                         "trials": len(v["trials"])} for k, v in tuned.items()},
         "accuracy": acc,
         "roofline": roofline,
         "cpu_baseline": cpu,

@@ -121,6 +121,26 @@ RL_API rl_status rl_dlu_inverse(size_t n, const double *lu, size_t lda, const ui
 RL_API rl_status rl_slu_det(size_t n, const float *lu, size_t lda, const uint64_t *perm, float *det);
 RL_API rl_status rl_dlu_det(size_t n, const double *lu, size_t lda, const uint64_t *perm, double *det);
 
+/* ------------------------------------------------------------------- FullPivLu -- */
+/* FullPivLu::decompose (src/matrix/decomposition/lu.rs:385-430): complete pivoting, A (n
+ * x n, in place) becomes the compact LU and p, q receive the stored row and column
+ * permutations (P A Q = L U, the reference's stored forms, lu.rs:425-429). Each pivot is
+ * the largest |a| of the trailing block, the first in row-major order on ties
+ * (select_pivot, lu.rs:364-382); a zero pivot ends the elimination (the reference's
+ * `break`, never an error). The elimination uses the reference's operations (multiplier
+ * by division, a - m * u without FMA), so LU, p and q are bit-identical to the
+ * reference's on every input. */
+RL_API rl_status rl_sfull_lu_decompose(size_t n, float *a, size_t lda, uint64_t *p, uint64_t *q);
+RL_API rl_status rl_dfull_lu_decompose(size_t n, double *a, size_t lda, uint64_t *p, uint64_t *q);
+/* FullPivLu::solve (lu.rs:480-486) for nrhs right-hand sides: B (n x nrhs, row stride
+ * ldb) is overwritten by X = Q U^-1 L^-1 P B; |u_ii| < epsilon returns RL_ERR_DIV_BY_ZERO
+ * (back_substitution, src/matrix/mod.rs:333-336), an invalid p or q
+ * RL_ERR_INVALID_PERMUTATION. */
+RL_API rl_status rl_sfull_lu_solve(size_t n, size_t nrhs, const float *lu, size_t lda, const uint64_t *p,
+                                   const uint64_t *q, float *b, size_t ldb);
+RL_API rl_status rl_dfull_lu_solve(size_t n, size_t nrhs, const double *lu, size_t lda, const uint64_t *p,
+                                   const uint64_t *q, double *b, size_t ldb);
+
 /* -------------------------------------------------------------------- Cholesky -- */
 /* Cholesky::decompose (src/matrix/decomposition/cholesky.rs:116-169): the lower triangle
  * of A (in place) becomes L with A = L L^T; the strict upper triangle is neither read nor
@@ -149,6 +169,30 @@ RL_API rl_status rl_sqr_first_k_columns(size_t m, size_t n, const float *qr, siz
                                  float *q, size_t ldq);
 RL_API rl_status rl_dqr_first_k_columns(size_t m, size_t n, const double *qr, size_t lda, const double *tau,
                                  size_t k, double *q, size_t ldq);
+/* HouseholderComposition::left_multiply_into (householder.rs:203-227): X <- Q X for the
+ * m x q matrix X (row stride ldx), Q = H_0 H_1 ... H_{p-1} of the compact storage from
+ * rl_*qr_decompose (m x n, p = min(m, n) reflectors, tau as there), the reflectors
+ * applied from the last to the first, without forming Q. */
+RL_API rl_status rl_sqr_q_apply(size_t m, size_t n, const float *qr, size_t lda, const float *tau, size_t q, float *x,
+                                size_t ldx);
+RL_API rl_status rl_dqr_q_apply(size_t m, size_t n, const double *qr, size_t lda, const double *tau, size_t q,
+                                double *x, size_t ldx);
+/* X <- Q^T X, the reflectors from the first to the last: the q1^T * b step of the
+ * least-squares composition (qr.rs:250-275 unpack_thin, then &Matrix * &Vector,
+ * src/matrix/impl_ops.rs:298-314, on the transpose) without forming Q. */
+RL_API rl_status rl_sqr_q_apply_t(size_t m, size_t n, const float *qr, size_t lda, const float *tau, size_t q,
+                                  float *x, size_t ldx);
+RL_API rl_status rl_dqr_q_apply_t(size_t m, size_t n, const double *qr, size_t lda, const double *tau, size_t q,
+                                  double *x, size_t ldx);
+/* BaseMatrix::solve_u_triangular (src/matrix/base/mod.rs:1015-1024, back_substitution
+ * src/matrix/mod.rs:318-357) and solve_l_triangular (base/mod.rs:1058-1067,
+ * forward_substitution src/matrix/mod.rs:363-398): T X = B for an n x n triangle (the
+ * other triangle's values are ignored), B n x nrhs overwritten by X; |t_ii| < epsilon returns
+ * RL_ERR_DIV_BY_ZERO as the reference's Err(DivByZero). */
+RL_API rl_status rl_strsv_upper(size_t n, size_t nrhs, const float *u, size_t ldu, float *b, size_t ldb);
+RL_API rl_status rl_dtrsv_upper(size_t n, size_t nrhs, const double *u, size_t ldu, double *b, size_t ldb);
+RL_API rl_status rl_strsv_lower(size_t n, size_t nrhs, const float *l, size_t ldl, float *b, size_t ldb);
+RL_API rl_status rl_dtrsv_lower(size_t n, size_t nrhs, const double *l, size_t ldl, double *b, size_t ldb);
 /* Least squares min ||A x - b||_2 for m >= n (no routine in the reference; it is the
  * composition unpack_thin -> q1^T b -> r1.solve_u_triangular, qr.rs:250-275,
  * src/matrix/base/mod.rs:1015-1024). A is consumed, b has m entries, x receives n.
@@ -239,6 +283,21 @@ RL_API rl_status rl_dsolve_mixed(size_t n, size_t nrhs, int kind, const double *
                                  size_t ldb, double *x, size_t ldx, rl_solve_info *info);
 RL_API rl_status rl_dsolve_fp64_dev(size_t n, size_t nrhs, int kind, const double *a, size_t lda, const double *b,
                                     size_t ldb, double *x, size_t ldx, rl_solve_info *info, void *stream);
+
+/* Resident factorisations for repeated solves with new right-hand sides. The replaced
+ * reference pattern is one `PartialPivLu::decompose(a)?` / `Cholesky::decompose(a)?`
+ * (lu.rs:163-194, cholesky.rs:116-169) followed by many `solve(b)` calls (lu.rs:231-244,
+ * cholesky.rs:194-202); here the factor stays on the device. rl_factor_create copies the
+ * device matrix A (n x n, row stride lda) and factors it in FP32 (mixed precision, as
+ * rl_dsolve_mixed); rl_factor_solve gives f64-accurate X for device B (n x nrhs) with
+ * FP64 refinement / GMRES-IR, building and keeping the FP64 factor if a solve needs it.
+ * Device pointers; both synchronise `stream` (the host reads the stopping test). Solves
+ * against one factor from several threads are serialised. */
+typedef struct rl_factor rl_factor;
+RL_API rl_status rl_factor_create(rl_factor **factor, int kind, size_t n, const double *a, size_t lda, void *stream);
+RL_API rl_status rl_factor_solve(rl_factor *factor, size_t nrhs, const double *b, size_t ldb, double *x, size_t ldx,
+                                 rl_solve_info *info, void *stream);
+RL_API rl_status rl_factor_destroy(rl_factor *factor);
 
 /* Least squares min ||A x - b||_2 (m >= n, one right-hand side) in mixed precision: the
  * f64 result of HouseholderQr::decompose(a) and the composition Q^T b, R x = (Q^T b)[0:n]

@@ -54,6 +54,9 @@ for sfx, ct in (("d", C.c_double), ("s", C.c_float)):
         ("or_qr_decompose", None, [_sz, _sz, _vp, _sz, _vp]),
         ("or_qr_first_k_columns", None, [_sz, _sz, _vp, _sz, _vp, _sz, _vp, _sz]),
         ("or_qr_q_left_multiply", None, [_sz, _sz, _vp, _sz, _vp, _sz, _vp, _sz]),
+        ("or_qr_qt_left_multiply", None, [_sz, _sz, _vp, _sz, _vp, _sz, _vp, _sz]),
+        ("or_full_lu_decompose", None, [_sz, _vp, _sz, _vp, _vp, _vp, _vp]),
+        ("or_full_lu_solve", C.c_int, [_sz, _vp, _sz, _vp, _vp, _vp]),
         ("or_qr_lstsq", C.c_int, [_sz, _sz, _vp, _sz, _vp, _vp]),
         ("or_gemm_mt", None, [_sz, _sz, _sz, _vp, _sz, _vp, _sz, _vp, _sz, C.c_int]),
         ("or_lu_decompose_mt", C.c_int, [_sz, _vp, _sz, _vp, _vp, C.c_int]),
@@ -153,6 +156,49 @@ def solve_columns(lu, perm, b, threads=1):
     st = _f(lu, "or_solve_columns_mt")(n, _p(lu), max(n, 1), _p(pp) if pp is not None else None, x.shape[1], _p(x),
                                        max(x.shape[1], 1), threads)
     return x, st
+
+
+def full_lu_decompose(a):
+    """FullPivLu::decompose: returns (lu, p, q, piv_r, piv_c) (stored permutations and
+    the per-step pivot positions, -1 after a zero pivot ended the elimination)."""
+    lu = _m(a)
+    n = lu.shape[0]
+    p = np.zeros(max(n, 1), dtype=np.uint64)
+    q = np.zeros(max(n, 1), dtype=np.uint64)
+    pr = np.zeros(max(n, 1), dtype=np.int64)
+    pc = np.zeros(max(n, 1), dtype=np.int64)
+    _f(lu, "or_full_lu_decompose")(n, _p(lu), max(n, 1), _p(p), _p(q), _p(pr), _p(pc))
+    return lu, p[:n], q[:n], pr[:n], pc[:n]
+
+
+def full_lu_solve(lu, p, q, b):
+    lu = _m(lu)
+    x = _m(b, lu.dtype)
+    st = _f(lu, "or_full_lu_solve")(lu.shape[0], _p(lu), max(lu.shape[0], 1), _p(_m(p, np.uint64)),
+                                    _p(_m(q, np.uint64)), _p(x))
+    return x, st
+
+
+def full_lu_rank(lu):
+    """FullPivLu::rank (lu.rs:547-561): diagonal entries above |lu[0,0]| eps, counted up
+    to the first that is not."""
+    n = lu.shape[0]
+    eps = abs(lu[0, 0] if n else lu.dtype.type(1)) * np.finfo(lu.dtype).eps
+    r = 0
+    for i in range(n):
+        if abs(lu[i, i]) > eps:
+            r += 1
+        else:
+            break
+    return r
+
+
+def full_lu_is_invertible(lu):
+    """FullPivLu::is_invertible (lu.rs:582-593)."""
+    n = lu.shape[0]
+    if n == 0:
+        return True
+    return abs(lu[n - 1, n - 1]) > abs(lu[0, 0]) * np.finfo(lu.dtype).eps
 
 
 def lu_inverse(lu, perm):
@@ -265,6 +311,15 @@ def qr_q_left_multiply(qr, tau, x):
     tau = _m(tau if len(tau) else np.zeros(1), qr.dtype)
     x = _m(x, qr.dtype)
     _f(qr, "or_qr_q_left_multiply")(m, n, _p(qr), max(n, 1), _p(tau), x.shape[1], _p(x), max(x.shape[1], 1))
+    return x
+
+
+def qr_qt_left_multiply(qr, tau, x):
+    qr = _m(qr)
+    m, n = qr.shape
+    tau = _m(tau if len(tau) else np.zeros(1), qr.dtype)
+    x = _m(x, qr.dtype)
+    _f(qr, "or_qr_qt_left_multiply")(m, n, _p(qr), max(n, 1), _p(tau), x.shape[1], _p(x), max(x.shape[1], 1))
     return x
 
 

@@ -238,6 +238,83 @@ T FN(or_matrix_det)(size_t n, T *a, size_t lda) {
     return d;
 }
 
+/* ------------------------------------------------------------------ FullPivLu -- */
+
+/* FullPivLu::decompose (src/matrix/decomposition/lu.rs:385-430) with select_pivot
+ * (lu.rs:364-382): at step `index` the pivot is the largest |a| of the trailing block,
+ * scanned row by row from (index, index) with a strict > (the first maximum in row-major
+ * order wins; a NaN never wins); a zero pivot ends the elimination (`break`, never an
+ * error). Whole rows and whole columns are swapped (src/matrix/base/mod.rs:1394-1418,
+ * :1446-1463), the swaps recorded in p and q (permutation_matrix.rs:132-134), then
+ * gaussian_elimination (lu.rs:603-616). p_out / q_out (optional) receive the stored
+ * forms, the inverses of the accumulated permutations (lu.rs:425-429); piv_r / piv_c
+ * (optional) the pivot row and column of each step, -1 from a break on. */
+void FN(or_full_lu_decompose)(size_t n, T *a, size_t lda, uint64_t *p_out, uint64_t *q_out, int64_t *piv_r,
+                              int64_t *piv_c) {
+    uint64_t *p = (uint64_t *)malloc(((n) + 1) * sizeof(uint64_t));
+    uint64_t *q = (uint64_t *)malloc(((n) + 1) * sizeof(uint64_t));
+    for (size_t i = 0; i < n; i++) p[i] = q[i] = i;
+    for (size_t i = 0; i < n; i++) {
+        if (piv_r) piv_r[i] = -1;
+        if (piv_c) piv_c[i] = -1;
+    }
+    for (size_t index = 0; index < n; index++) {
+        size_t pr = index, pc = index;
+        T pv = a[index * lda + index];
+        for (size_t row = index; row < n; row++)
+            for (size_t col = index; col < n; col++) {
+                const T val = a[row * lda + col];
+                if (ABS(val) > ABS(pv)) {
+                    pv = val;
+                    pr = row;
+                    pc = col;
+                }
+            }
+        if (ABS(pv) == 0) break;
+        if (piv_r) piv_r[index] = (int64_t)pr;
+        if (piv_c) piv_c[index] = (int64_t)pc;
+        if (pr != index)
+            for (size_t j = 0; j < n; j++) {
+                const T t = a[index * lda + j];
+                a[index * lda + j] = a[pr * lda + j];
+                a[pr * lda + j] = t;
+            }
+        if (pc != index)
+            for (size_t i = 0; i < n; i++) {
+                const T t = a[i * lda + index];
+                a[i * lda + index] = a[i * lda + pc];
+                a[i * lda + pc] = t;
+            }
+        uint64_t t = p[index];
+        p[index] = p[pr];
+        p[pr] = t;
+        t = q[index];
+        q[index] = q[pc];
+        q[pc] = t;
+        FN(gaussian_elimination)(n, a, lda, index);
+    }
+    if (p_out)
+        for (size_t i = 0; i < n; i++) p_out[p[i]] = i;
+    if (q_out)
+        for (size_t i = 0; i < n; i++) q_out[q[i]] = i;
+    free(p);
+    free(q);
+}
+
+/* FullPivLu::solve (lu.rs:480-486): y = P b (buffer[p[i]] = b[i],
+ * permutation_matrix.rs:369-382), unit-lower forward and upper back substitution
+ * (DivByZero when |u_ii| < epsilon), x = Q y the same way with q. b is overwritten. */
+int FN(or_full_lu_solve)(size_t n, const T *lu, size_t lda, const uint64_t *p, const uint64_t *q, T *b) {
+    T *y = (T *)malloc(((n) + 1) * sizeof(T));
+    for (size_t i = 0; i < n; i++) y[p[i]] = b[i];
+    FN(lu_forward_substitution)(n, lu, lda, y);
+    const int st = FN(or_back_substitution)(n, lu, lda, y);
+    if (st == RL_OK)
+        for (size_t i = 0; i < n; i++) b[q[i]] = y[i];
+    free(y);
+    return st;
+}
+
 /* ------------------------------------------------------------------- Cholesky -- */
 
 /* Cholesky::decompose (src/matrix/decomposition/cholesky.rs:116-169), GVL 4.2.5 gaxpy
@@ -392,6 +469,25 @@ void FN(or_qr_q_left_multiply)(size_t m, size_t n, const T *qr, size_t lda, cons
     T *v = (T *)malloc(((m) + 1) * sizeof(T));
     T *u = (T *)malloc(((q) + 1) * sizeof(T));
     for (size_t jj = p; jj-- > 0;) {
+        const size_t mj = m - jj;
+        for (size_t i = 0; i < mj; i++) v[i] = qr[(jj + i) * lda + jj];
+        v[0] = 1;
+        FN(or_house_apply)(mj, q, x + jj * ldx, ldx, v, tau[jj], u);
+    }
+    free(v);
+    free(u);
+}
+
+/* X <- Q^T X: the same reflectors as or_qr_q_left_multiply (buffered_left_multiply_into,
+ * householder.rs:100-130, each loaded by load_house_from_col, :271-284) applied from the
+ * first to the last. The reference has no such method; Q^T X is what the least-squares
+ * composition computes as q1^T * b (qr.rs:250-275 then impl_ops.rs:298-314). */
+void FN(or_qr_qt_left_multiply)(size_t m, size_t n, const T *qr, size_t lda, const T *tau, size_t q, T *x,
+                                size_t ldx) {
+    const size_t p = m < n ? m : n;
+    T *v = (T *)malloc(((m) + 1) * sizeof(T));
+    T *u = (T *)malloc(((q) + 1) * sizeof(T));
+    for (size_t jj = 0; jj < p; jj++) {
         const size_t mj = m - jj;
         for (size_t i = 0; i < mj; i++) v[i] = qr[(jj + i) * lda + jj];
         v[0] = 1;

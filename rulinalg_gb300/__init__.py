@@ -3,8 +3,9 @@ HouseholderQr with solve/det/inverse) as hand-written sm_103a CUDA behind a C AB
 (include/rulinalg_gb300.h). Importing loads librulinalg_gb300.so; there is no CPU path."""
 from ._lib import lib, LIB_PATH  # noqa: F401  (raises ImportError when the library is not built)
 from .api import (  # noqa: F401
-    Cholesky, DeviceError, HouseholderQr, LUP, PartialPivLu, PermutationMatrix, QR, RulinalgError,
-    RulinalgPanic, ThinQR, det, inverse, least_squares, lstsq_mixed, mat_mul, solve, solve_mixed,
+    Cholesky, DeviceError, FullPivLu, HouseholderComposition, HouseholderQr, LUP, LUPQ, PartialPivLu, PermutationMatrix, QR,
+    ResidentFactor, RulinalgError, RulinalgPanic, ThinQR, det, inverse, least_squares, lstsq_mixed, mat_mul, solve,
+    solve_l_triangular, solve_mixed, solve_u_triangular,
 )
 from .batch import BatchPlan, KIND_CHOLESKY, KIND_LU, PREC_FP32, PREC_FP64, PREC_MIXED  # noqa: F401
 from .server import REQ_CHOLESKY, REQ_LSTSQ, REQ_LU, REQ_RESOLVE, Server  # noqa: F401

@@ -51,6 +51,10 @@ SIGNATURES = {
     "rl_dlu_inverse": (st, [sz, f64p, sz, u64p, f64p, sz]),
     "rl_slu_det": (st, [sz, f32p, sz, u64p, f32p]),
     "rl_dlu_det": (st, [sz, f64p, sz, u64p, f64p]),
+    "rl_sfull_lu_decompose": (st, [sz, f32p, sz, u64p, u64p]),
+    "rl_dfull_lu_decompose": (st, [sz, f64p, sz, u64p, u64p]),
+    "rl_sfull_lu_solve": (st, [sz, sz, f32p, sz, u64p, u64p, f32p, sz]),
+    "rl_dfull_lu_solve": (st, [sz, sz, f64p, sz, u64p, u64p, f64p, sz]),
     "rl_scholesky_decompose": (st, [sz, f32p, sz]),
     "rl_dcholesky_decompose": (st, [sz, f64p, sz]),
     "rl_scholesky_solve": (st, [sz, sz, f32p, sz, f32p, sz]),
@@ -63,6 +67,17 @@ SIGNATURES = {
     "rl_dqr_decompose": (st, [sz, sz, f64p, sz, f64p]),
     "rl_sqr_first_k_columns": (st, [sz, sz, f32p, sz, f32p, sz, f32p, sz]),
     "rl_dqr_first_k_columns": (st, [sz, sz, f64p, sz, f64p, sz, f64p, sz]),
+    "rl_sqr_q_apply": (st, [sz, sz, f32p, sz, f32p, sz, f32p, sz]),
+    "rl_dqr_q_apply": (st, [sz, sz, f64p, sz, f64p, sz, f64p, sz]),
+    "rl_sqr_q_apply_t": (st, [sz, sz, f32p, sz, f32p, sz, f32p, sz]),
+    "rl_dqr_q_apply_t": (st, [sz, sz, f64p, sz, f64p, sz, f64p, sz]),
+    "rl_strsv_upper": (st, [sz, sz, f32p, sz, f32p, sz]),
+    "rl_dtrsv_upper": (st, [sz, sz, f64p, sz, f64p, sz]),
+    "rl_strsv_lower": (st, [sz, sz, f32p, sz, f32p, sz]),
+    "rl_dtrsv_lower": (st, [sz, sz, f64p, sz, f64p, sz]),
+    "rl_factor_create": (st, [C.POINTER(vp), C.c_int, sz, vp, sz, vp]),
+    "rl_factor_solve": (st, [vp, sz, vp, sz, vp, sz, vp, vp]),
+    "rl_factor_destroy": (st, [vp]),
     "rl_sqr_least_squares": (st, [sz, sz, f32p, sz, f32p, f32p]),
     "rl_dqr_least_squares": (st, [sz, sz, f64p, sz, f64p, f64p]),
     "rl_smatrix_solve": (st, [sz, f32p, sz, f32p]),

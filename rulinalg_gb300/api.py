@@ -5,6 +5,8 @@ Names, argument meaning and error behaviour follow the reference crate:
   * `PartialPivLu.decompose(m)` ...     <- src/matrix/decomposition/lu.rs:130-300
   * `Cholesky.decompose(m)` ...         <- src/matrix/decomposition/cholesky.rs:93-246
   * `HouseholderQr.decompose(m)` ...    <- src/matrix/decomposition/qr.rs:171-315
+  * `HouseholderQr.q().left_multiply_into(x)` <- householder.rs:203-227
+  * `solve_u_triangular / solve_l_triangular` <- src/matrix/base/mod.rs:1015-1067
   * `solve/inverse/det(m, ...)`         <- Matrix::solve/inverse/det (src/matrix/impl_mat.rs:354-427)
 A numerical failure raises `RulinalgError` with the reference's ErrorKind; a dimension
 misuse raises `RulinalgPanic` (the reference panics via assert!). Matrices are numpy
@@ -30,6 +32,7 @@ ERROR_KINDS = {
     5: "ScalarConversionFailure",
     6: "InvalidPermutation",
 }
+DIV_BY_ZERO = 4
 RL_ERR_SHAPE = 16
 RL_ERR_NO_DEVICE = 33
 
@@ -153,6 +156,21 @@ class PermutationMatrix:
         inv[self.perm.astype(np.int64)] = np.arange(len(self.perm), dtype=self.perm.dtype)
         return PermutationMatrix(inv)
 
+    def det(self) -> float:
+        """PermutationMatrix::det (permutation_matrix.rs:254-260): +1 for an even
+        permutation, -1 for an odd one (parity by cycle resolution, :216-234)."""
+        perm = [int(v) for v in self.perm]
+        odd = False
+        for i in range(len(perm)):
+            target = perm[i]
+            while i != target:
+                nxt = perm[target]
+                odd = not odd
+                perm[target] = target
+                target = nxt
+            perm[i] = i
+        return -1.0 if odd else 1.0
+
 
 @dataclass
 class LUP:
@@ -207,6 +225,85 @@ class PartialPivLu:
         np.fill_diagonal(l, 1)
         u = np.triu(self.lu)
         return LUP(l, u, self.p)
+
+
+@dataclass
+class LUPQ:
+    l: np.ndarray
+    u: np.ndarray
+    p: "PermutationMatrix"
+    q: "PermutationMatrix"
+
+
+class FullPivLu:
+    """PAQ = LU with complete pivoting (lu.rs:303-599), factored on the GPU; the factors
+    and permutations are bit-identical to the reference's."""
+
+    def __init__(self, lu: np.ndarray, p: np.ndarray, q: np.ndarray):
+        self.lu = lu
+        self.p = PermutationMatrix(p)
+        self.q = PermutationMatrix(q)
+
+    @staticmethod
+    def decompose(matrix) -> "FullPivLu":
+        a = _mat(matrix).copy()
+        n = a.shape[1]
+        if a.shape[0] != n:
+            raise RulinalgPanic("Matrix must be square for LU decomposition.")  # lu.rs:386-388
+        p = np.arange(n, dtype=np.uint64)
+        q = np.arange(n, dtype=np.uint64)
+        _check(_fn(_prefix(a), "full_lu_decompose")(n, _ptr(a), max(n, 1), _ptr(p), _ptr(q)))
+        return FullPivLu(a, p, q)
+
+    def solve(self, b) -> np.ndarray:
+        n = self.lu.shape[0]
+        b = np.array(b, dtype=self.lu.dtype, copy=True, order="C")
+        if b.shape[0] != n:
+            raise RulinalgPanic("Right-hand side vector must have compatible size.")  # lu.rs:481
+        nrhs = 1 if b.ndim == 1 else b.shape[1]
+        _check(_fn(_prefix(self.lu), "full_lu_solve")(n, nrhs, _ptr(self.lu), max(n, 1), _ptr(self.p.perm),
+                                                     _ptr(self.q.perm), _ptr(b), max(nrhs, 1)))
+        return b
+
+    def _epsilon(self) -> float:
+        """|lu[0, 0]| eps (lu.rs:595-597); 1 eps for an empty matrix."""
+        n = self.lu.shape[0]
+        return abs(float(self.lu[0, 0]) if n else 1.0) * float(np.finfo(self.lu.dtype).eps)
+
+    def rank(self) -> int:
+        """FullPivLu::rank (lu.rs:547-561)."""
+        eps, r = self._epsilon(), 0
+        for i in range(self.lu.shape[0]):
+            if abs(float(self.lu[i, i])) > eps:
+                r += 1
+            else:
+                break
+        return r
+
+    def is_invertible(self) -> bool:
+        """FullPivLu::is_invertible (lu.rs:582-593)."""
+        n = self.lu.shape[0]
+        return True if n == 0 else abs(float(self.lu[n - 1, n - 1])) > self._epsilon()
+
+    def det(self) -> float:
+        """FullPivLu::det (lu.rs:512-524): p_det * (fold of diag(U)) * q_det."""
+        u_det = self.lu.dtype.type(1)
+        for i in range(self.lu.shape[0]):
+            u_det = u_det * self.lu[i, i]
+        return float(self.p.det() * u_det * self.q.det())
+
+    def inverse(self) -> np.ndarray:
+        """FullPivLu::inverse (lu.rs:493-509): DivByZero when not invertible."""
+        n = self.lu.shape[0]
+        if not self.is_invertible():
+            raise RulinalgError(DIV_BY_ZERO)
+        return self.solve(np.eye(n, dtype=self.lu.dtype))
+
+    def unpack(self) -> LUPQ:
+        """`Decomposition::unpack` (lu.rs:345-361): unit lower L, upper U, P, Q."""
+        l = np.tril(self.lu, -1)
+        np.fill_diagonal(l, 1)
+        return LUPQ(l, np.triu(self.lu), self.p, self.q)
 
 
 class Cholesky:
@@ -288,6 +385,10 @@ class HouseholderQr:
                                                           max(k, 1)))
         return q
 
+    def q(self) -> "HouseholderComposition":
+        """HouseholderQr::q (qr.rs:228-230): Q as a composition of the stored reflectors."""
+        return HouseholderComposition(self)
+
     def unpack(self) -> QR:
         m = self.qr.shape[0]
         return QR(self.first_k_columns(m), np.triu(self.qr))
@@ -298,6 +399,101 @@ class HouseholderQr:
             qr = self.unpack()
             return ThinQR(qr.q, qr.r)
         return ThinQR(self.first_k_columns(n), np.triu(self.qr[:n, :]))
+
+
+class HouseholderComposition:
+    """Q = H_0 H_1 ... H_{p-1} of a compact QR (householder.rs:177-284), applied on the GPU
+    without forming Q."""
+
+    def __init__(self, qr: HouseholderQr):
+        self._qr = qr
+
+    def _apply(self, x, trans: bool) -> None:
+        st = self._qr
+        m, n = st.qr.shape
+        if not isinstance(x, np.ndarray) or x.dtype != st.qr.dtype or x.ndim != 2 or not x.flags.c_contiguous:
+            raise RulinalgPanic("expected a C-contiguous matrix of the factor's type")
+        if x.shape[0] != m:
+            raise RulinalgPanic("Number of rows of Q and X must agree")  # householder.rs:205
+        tau = st.tau if len(st.tau) else np.zeros(1, dtype=st.qr.dtype)
+        name = "qr_q_apply_t" if trans else "qr_q_apply"
+        _check(_fn(_prefix(st.qr), name)(m, n, _ptr(st.qr), max(n, 1), _ptr(tau), x.shape[1], _ptr(x),
+                                        max(x.shape[1], 1)))
+
+    def left_multiply_into(self, x: np.ndarray) -> None:
+        """HouseholderComposition::left_multiply_into (householder.rs:203-227): x <- Q x in place."""
+        self._apply(x, False)
+
+    def left_multiply_into_transposed(self, x: np.ndarray) -> None:
+        """x <- Q^T x in place (the q1^T b of least squares, without forming Q)."""
+        self._apply(x, True)
+
+    def first_k_columns(self, k: int) -> np.ndarray:
+        """HouseholderComposition::first_k_columns (householder.rs:235-268)."""
+        return self._qr.first_k_columns(k)
+
+
+def _triangular(t, b, upper: bool) -> np.ndarray:
+    t = _mat(t)
+    n = t.shape[0]
+    if t.shape[1] != n:
+        raise RulinalgPanic("Matrix must be square to solve a triangular system.")
+    x = np.array(b, dtype=t.dtype, copy=True, order="C")
+    if x.shape[0] != n:
+        raise RulinalgPanic("Vector size must match the number of rows of the matrix.")
+    nrhs = 1 if x.ndim == 1 else x.shape[1]
+    _check(_fn(_prefix(t), "trsv_upper" if upper else "trsv_lower")(n, nrhs, _ptr(t), max(n, 1), _ptr(x),
+                                                                   max(nrhs, 1)))
+    return x
+
+
+def solve_u_triangular(u, y) -> np.ndarray:
+    """BaseMatrix::solve_u_triangular (base/mod.rs:1015-1024): back substitution with the
+    upper triangle of u (its strict lower part is ignored); DivByZero for |u_ii| < eps."""
+    return _triangular(u, y, True)
+
+
+def solve_l_triangular(l, y) -> np.ndarray:
+    """BaseMatrix::solve_l_triangular (base/mod.rs:1058-1067): forward substitution with the
+    lower triangle of l; DivByZero for |l_ii| < eps."""
+    return _triangular(l, y, False)
+
+
+class ResidentFactor:
+    """A device-resident factorisation (rl_factor_*) for repeated f64-accurate solves:
+    `a` and each `b` / `x` are device buffers given as torch CUDA tensors (float64,
+    row-major contiguous); `kind` is "lu" or "cholesky"."""
+
+    def __init__(self, a, kind: str = "lu", stream: int = 0):
+        n = a.shape[0]
+        if a.shape != (n, n) or not a.is_contiguous():
+            raise RulinalgPanic("Matrix must be square and contiguous")
+        self.n = n
+        h = C.c_void_p()
+        _check(lib.rl_factor_create(C.byref(h), 1 if kind == "cholesky" else 0, n, a.data_ptr(), n, stream or None))
+        self._h = h
+
+    def solve(self, b, x, stream: int = 0) -> dict:
+        from ._lib import SolveInfo
+        nrhs = 1 if b.dim() == 1 else b.shape[1]
+        if b.shape[0] != self.n or x.shape != b.shape or not b.is_contiguous() or not x.is_contiguous():
+            raise RulinalgPanic("Right-hand side and solution must be n x nrhs and contiguous")
+        info = SolveInfo()
+        _check(lib.rl_factor_solve(self._h, nrhs, b.data_ptr(), nrhs, x.data_ptr(), nrhs, C.byref(info),
+                                   stream or None))
+        return {"iters": info.iters, "gmres_iters": info.gmres_iters, "path": PATHS.get(info.path, info.path),
+                "berr": info.berr}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib.rl_factor_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def least_squares(matrix, b) -> np.ndarray:

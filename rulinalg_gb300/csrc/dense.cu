@@ -251,6 +251,53 @@ rl_status qr_first_k_host(size_t m, size_t n, const T *qr, size_t lda, const T *
 }
 
 template <class T>
+rl_status qr_apply_q_host(size_t m, size_t n, const T *qr, size_t lda, const T *tau, size_t q, T *x, size_t ldx,
+                          bool trans) {
+    if (m == 0 || q == 0) return RL_OK;
+    const size_t p = std::min(m, n);
+    if (!qr || !x || (p && !tau) || lda < n || ldx < q || !fits_int(m) || !fits_int(n) || !fits_int(q))
+        return RL_ERR_INVALID_ARG;
+    RL_TRY(ensure_device());
+    cudaStream_t s = cudaStreamPerThread;
+    DevBuf<T> dA, dt, dX;
+    RL_TRY(dA.alloc(std::max<size_t>(1, m * n), s));
+    RL_TRY(dt.alloc(std::max<size_t>(1, p), s));
+    RL_TRY(dX.alloc(m * q, s));
+    RL_TRY(copy_h2d(dA.p, n, qr, lda, m, n, s));
+    if (p) RL_TRY_CUDA(cudaMemcpyAsync(dt.p, tau, p * sizeof(T), cudaMemcpyHostToDevice, s));
+    RL_TRY(copy_h2d(dX.p, q, x, ldx, m, q, s));
+    RL_TRY(qr_apply_q_dev<T>(dA.p, (long long)n, (int)m, (int)n, dt.p, (int)q, dX.p, (long long)q, trans, s));
+    RL_TRY(copy_d2h(x, ldx, dX.p, q, m, q, s));
+    RL_TRY_CUDA(cudaStreamSynchronize(s));
+    return RL_OK;
+}
+
+// U X = B (upper = true, back_substitution) or L X = B (forward_substitution) for an
+// n x n triangle (the other triangle's values are ignored) and n x nrhs B, overwritten
+// by X.
+template <class T>
+rl_status trsv_host(size_t n, size_t nrhs, const T *t, size_t ldt, T *b, size_t ldb, bool upper) {
+    if (n == 0 || nrhs == 0) return RL_OK;
+    if (!t || !b || ldt < n || ldb < nrhs || !fits_int(n) || !fits_int(nrhs)) return RL_ERR_INVALID_ARG;
+    RL_TRY(ensure_device());
+    cudaStream_t s = cudaStreamPerThread;
+    DevBuf<T> dT, dB;
+    DevBuf<int> st;
+    RL_TRY(dT.alloc(n * n, s));
+    RL_TRY(dB.alloc(n * nrhs, s));
+    RL_TRY(st.alloc(1, s));
+    RL_TRY_CUDA(cudaMemsetAsync(st.p, 0, sizeof(int), s));
+    RL_TRY(copy_h2d(dT.p, n, t, ldt, n, n, s));
+    RL_TRY(copy_h2d(dB.p, nrhs, b, ldb, n, nrhs, s));
+    RL_TRY(tri_solve_dev<T>(dT.p, (long long)n, (int)n, dB.p, (long long)nrhs, (int)nrhs, upper ? 2 : 1, st.p, s));
+    const rl_status r = read_status<T>(st.p, s);
+    if (r != RL_OK) return r;
+    RL_TRY(copy_d2h(b, ldb, dB.p, nrhs, n, nrhs, s));
+    RL_TRY_CUDA(cudaStreamSynchronize(s));
+    return RL_OK;
+}
+
+template <class T>
 rl_status qr_lstsq_host(size_t m, size_t n, T *a, size_t lda, const T *b, T *x) {
     if (m < n) return RL_ERR_SHAPE;
     if (n == 0) return RL_OK;
@@ -483,6 +530,34 @@ rl_status rl_sqr_first_k_columns(size_t m, size_t n, const float *qr, size_t lda
 rl_status rl_dqr_first_k_columns(size_t m, size_t n, const double *qr, size_t lda, const double *tau, size_t k,
                                  double *q, size_t ldq) {
     return qr_first_k_host<double>(m, n, qr, lda, tau, k, q, ldq);
+}
+rl_status rl_sqr_q_apply(size_t m, size_t n, const float *qr, size_t lda, const float *tau, size_t q, float *x,
+                         size_t ldx) {
+    return qr_apply_q_host<float>(m, n, qr, lda, tau, q, x, ldx, false);
+}
+rl_status rl_dqr_q_apply(size_t m, size_t n, const double *qr, size_t lda, const double *tau, size_t q, double *x,
+                         size_t ldx) {
+    return qr_apply_q_host<double>(m, n, qr, lda, tau, q, x, ldx, false);
+}
+rl_status rl_sqr_q_apply_t(size_t m, size_t n, const float *qr, size_t lda, const float *tau, size_t q, float *x,
+                           size_t ldx) {
+    return qr_apply_q_host<float>(m, n, qr, lda, tau, q, x, ldx, true);
+}
+rl_status rl_dqr_q_apply_t(size_t m, size_t n, const double *qr, size_t lda, const double *tau, size_t q, double *x,
+                           size_t ldx) {
+    return qr_apply_q_host<double>(m, n, qr, lda, tau, q, x, ldx, true);
+}
+rl_status rl_strsv_upper(size_t n, size_t nrhs, const float *u, size_t ldu, float *b, size_t ldb) {
+    return trsv_host<float>(n, nrhs, u, ldu, b, ldb, true);
+}
+rl_status rl_dtrsv_upper(size_t n, size_t nrhs, const double *u, size_t ldu, double *b, size_t ldb) {
+    return trsv_host<double>(n, nrhs, u, ldu, b, ldb, true);
+}
+rl_status rl_strsv_lower(size_t n, size_t nrhs, const float *l, size_t ldl, float *b, size_t ldb) {
+    return trsv_host<float>(n, nrhs, l, ldl, b, ldb, false);
+}
+rl_status rl_dtrsv_lower(size_t n, size_t nrhs, const double *l, size_t ldl, double *b, size_t ldb) {
+    return trsv_host<double>(n, nrhs, l, ldl, b, ldb, false);
 }
 rl_status rl_sqr_least_squares(size_t m, size_t n, float *a, size_t lda, const float *b, float *x) {
     return qr_lstsq_host<float>(m, n, a, lda, b, x);

@@ -406,6 +406,44 @@ rl_status qr_first_k_dev(const T *QR, long long lda, int m, int n, const T *tau,
     return RL_OK;
 }
 
+// X <- Q X (trans = false) or X <- Q^T X (trans = true) for the m x q matrix X (row
+// stride ldx), Q = H_0 H_1 ... H_{p-1} from the compact QR (m x n, p = min(m, n)):
+// HouseholderComposition::left_multiply_into (householder.rs:203-227) applies the
+// reflectors from the last to the first, Q^T takes them from the first to the last.
+// Per 64-reflector panel (compact WY, Q_i = I - V T V^T): X[k0:, :] -= V (op(T) (V^T X[k0:, :]))
+// with op(T) = T for Q, T^T for Q^T.
+template <class T>
+rl_status qr_apply_q_dev(const T *QR, long long lda, int m, int n, const T *tau, int q, T *X, long long ldx, bool trans,
+                         cudaStream_t s) {
+    const int p = std::min(m, n);
+    if (m <= 0 || q <= 0 || p <= 0) return RL_OK;
+    constexpr int NB = PanelNB<T>::value;
+    DevBuf<T> V, Gp, Tm, W1, W2;
+    RL_TRY(V.alloc((size_t)m * NB, s));
+    const int max_parts = ceil_div(m, kGramRows);
+    RL_TRY(Gp.alloc((size_t)max_parts * 64 * 64, s));
+    RL_TRY(Tm.alloc(NB * NB, s));
+    RL_TRY(W1.alloc((size_t)NB * q, s));
+    RL_TRY(W2.alloc((size_t)NB * q, s));
+    const int last = ((p - 1) / NB) * NB;
+    for (int i = 0; i <= last / NB; i++) {
+        const int k0 = trans ? i * NB : last - i * NB;
+        const int kb = std::min(NB, p - k0), mrows = m - k0;
+        const T *P = QR + (long long)k0 * lda + k0;
+        const long long mkb = (long long)mrows * kb;
+        RL_LAUNCH(extract_v_kernel<T>, (int)((mkb + 255) / 256), 256, 0, s, P, lda, mrows, kb, V.p);
+        RL_TRY(block_t_factor<T>(V.p, mrows, kb, tau + k0, Gp.p, max_parts, Tm.p, s));
+        T *X2 = X + (long long)k0 * ldx;
+        RL_TRY((gemm<T, true, false>(kb, q, mrows, T(1), V.p, kb, X2, ldx, T(0), W1.p, q, s)));
+        if (trans)
+            RL_TRY((gemm<T, true, false>(kb, q, kb, T(1), Tm.p, kb, W1.p, q, T(0), W2.p, q, s)));
+        else
+            RL_TRY((gemm<T, false, false>(kb, q, kb, T(1), Tm.p, kb, W1.p, q, T(0), W2.p, q, s)));
+        RL_TRY((gemm<T, false, false>(mrows, q, kb, T(-1), V.p, kb, W2.p, q, T(1), X2, ldx, s)));
+    }
+    return RL_OK;
+}
+
 // Blocked triangular solve op(A) X = Y in place (A n x n, Y n x nrhs).
 // mode 0: unit lower, 1: lower, 2: upper, 3: L^T with L lower. |d_ii| < eps is
 // recorded as RL_ERR_DIV_BY_ZERO in *dstatus. A may be stored in a narrower type TA than

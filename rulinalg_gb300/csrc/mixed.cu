@@ -2,6 +2,8 @@
 // residual / update / backward-error stopping test, GMRES-IR when plain refinement
 // stalls (FP64 GMRES left-preconditioned by the FP32 factors), FP64 refactor when that
 // fails too. Plus the plain FP64 GPU solve used as its baseline.
+#include <mutex>
+
 #include "mixed_ops.cuh"
 
 namespace rl {
@@ -30,7 +32,57 @@ rl_status check_args(size_t n, size_t nrhs, int kind, const void *a, size_t lda,
 
 using namespace rl;
 
+// A resident factorisation: MixedFactor owns its device copy of A (FP64, for the
+// residuals), the FP32 factor and, once a solve needed it, the FP64 factor.
+struct rl_factor {
+    MixedFactor f;
+    std::mutex mu;  // solves against one factor are serialised (the FP64 factor is built lazily)
+};
+
 extern "C" {
+
+rl_status rl_factor_create(rl_factor **out, int kind, size_t n, const double *a, size_t lda, void *stream) {
+    if (!out || (kind != RL_KIND_LU && kind != RL_KIND_CHOLESKY)) return RL_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (n == 0 || !a || lda < n || n > (size_t)INT32_MAX) return RL_ERR_INVALID_ARG;
+    RL_TRY(ensure_device());
+    cudaStream_t s = resolve_stream(stream);
+    auto *h = new rl_factor();
+    const rl_status st = h->f.factor(a, (long long)lda, (int)n, kind, true, s);
+    if (st != RL_OK) {
+        cudaStreamSynchronize(s);
+        delete h;
+        return st;
+    }
+    *out = h;
+    return RL_OK;
+}
+
+rl_status rl_factor_solve(rl_factor *h, size_t nrhs, const double *b, size_t ldb, double *x, size_t ldx,
+                          rl_solve_info *info, void *stream) {
+    if (!h) return RL_ERR_INVALID_ARG;
+    SolveOut o;
+    if (nrhs == 0) {
+        fill_info(info, o);
+        return RL_OK;
+    }
+    if (!b || !x || ldb < nrhs || ldx < nrhs || nrhs > (size_t)INT32_MAX) return RL_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    RL_TRY(h->f.solve(b, (long long)ldb, x, (long long)ldx, (int)nrhs, o, resolve_stream(stream)));
+    fill_info(info, o);
+    return RL_OK;
+}
+
+rl_status rl_factor_destroy(rl_factor *h) {
+    if (!h) return RL_OK;
+    {
+        std::lock_guard<std::mutex> lk(h->mu);
+        cudaStreamSynchronize(h->f.home);
+        h->f.release();
+    }
+    delete h;
+    return RL_OK;
+}
 
 rl_status rl_dsolve_mixed_dev(size_t n, size_t nrhs, int kind, const double *a, size_t lda, const double *b, size_t ldb,
                               double *x, size_t ldx, rl_solve_info *info, void *stream) {

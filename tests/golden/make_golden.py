@@ -106,6 +106,13 @@ def main(ref: Path) -> None:
     add("lu_singular_4x4", lu, 761, 766, ["a"], error="DivByZero")
     add("lu_forward_substitution", lu, 869, 887, ["lu0", "b0", "lu1", "b1", "x1", "lu2", "b2", "x2"])
     add("solve_poisson_9x9", tm, 5, 19, ["a", "b", "x"], abs_tol=1e-8)
+    # FullPivLu
+    add("full_lu_reconstruct_4x4", lu, 898, 901, ["a"])
+    add("full_lu_singular_rank3", lu, 916, 919, ["a"], rank=3)
+    add("full_lu_solve_4x4", lu, 947, 952, ["a", "b", "x"], ulp_tol=100)
+    add("full_lu_inverse_4x4", lu, 965, 973, ["a", "inv"])
+    add("full_lu_noninvertible_3x3", lu, 982, 984, ["a"], error="DivByZero")
+    add("full_lu_doc_rank2", lu, 537, 539, ["a"], rank=2)
     # Matrix::solve / det
     dets = _scalars(span(im, 652, 677), r"assert(?:_scalar)?_eq!\([a-z], ([-0-9.]+)")
     add("matrix_det", im, 649, 675, ["a2", "c3", "e5", "g4"], dets=dets)

@@ -52,3 +52,15 @@ def test_lu_unpack_matches_reference_3x3(rl, golden):
     # unit lower / upper structure
     assert np.array_equal(np.diag(lup.l), np.ones(3)) and not np.triu(lup.l, 1).any()
     assert not np.tril(lup.u, -1).any()
+
+
+def test_autotune_key_follows_the_size_histogram(rl):
+    """The autotuner's cache key: the same for batches with the same per-octave size
+    histogram, different when the histogram, the precision or the GPU changes."""
+    from rulinalg_gb300.autotune import batch_key
+    n1 = [8, 9, 100, 300, 300]
+    k1 = [0, 0, 1, 1, 0]
+    assert batch_key(n1, k1, 1, "GB300") == batch_key([15, 8, 127, 511, 256], k1, 1, "GB300")
+    assert batch_key(n1, k1, 1, "GB300") != batch_key(n1, [1, 0, 1, 1, 0], 1, "GB300")
+    assert batch_key(n1, k1, 1, "GB300") != batch_key(n1, k1, 0, "GB300")
+    assert batch_key(n1, k1, 1, "GB300") != batch_key(n1, k1, 1, "other")

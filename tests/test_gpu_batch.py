@@ -293,3 +293,35 @@ def test_config4_spd_f32(gpu):
         assert np.all(fe <= 2 * kappa_inf(ab) * (hb + host_berr(ab, bb, xob)))
         worst = max(worst, float(fe.max()))
     print(f"f32 SPD half: max berr {berr.max():.3e}, max forward error vs f64 oracle {worst:.3e}")
+
+
+def test_autotune_no_slower_than_defaults_and_cached(gpu, tmp_path):
+    """The autotuner times candidate launch shapes / size classes and keeps one no slower
+    than the defaults; a second call on a batch of the same shape comes from the cache;
+    the tuned plan still solves every system f64-accurately."""
+    import torch
+    from rulinalg_gb300 import autotune
+    from rulinalg_gb300.workloads import mixed_batch
+    from rulinalg_gb300 import _lib as L
+    saved = {k: gpu.tune_get(k) for k in (L.TUNE_BATCH_CTAS_PER_SM, L.TUNE_BATCH_WARP_COST, L.TUNE_UPLOAD_CHUNKS)}
+    dev = torch.device("cuda:0")
+    n, kind, a, b = mixed_batch(1500, 1500, seed=3, device=dev)
+    try:
+        r = autotune.tune(n, kind, gpu.PREC_MIXED, a, b, reps=2, cache=tmp_path / "tune.json")
+        assert not r["cached"] and r["ms"] <= r["default_ms"] and len(r["trials"]) >= 5
+        print(f"autotune: {r['choice']} {r['ms']:.2f} ms (defaults {r['default_ms']:.2f} ms)")
+        r2 = autotune.tune(n, kind, gpu.PREC_MIXED, a, b, cache=tmp_path / "tune.json")
+        assert r2["cached"] and r2["choice"] == r["choice"]
+        plan = gpu.BatchPlan(n, kind, gpu.PREC_MIXED)
+        x = torch.zeros_like(b)
+        info = torch.zeros(len(n), dtype=torch.int32, device=dev)
+        berr = torch.zeros(len(n), dtype=torch.float64, device=dev)
+        plan.solve_dev(a.data_ptr(), b.data_ptr(), x.data_ptr(), info.data_ptr(), 0, berr.data_ptr(),
+                       torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        plan.close()
+        assert bool((info == 0).all())
+        assert bool((berr.cpu() <= torch.from_numpy(n.astype(np.float64) * U64 * 10)).all())
+    finally:
+        for k, v in saved.items():
+            gpu.tune_set(k, v)

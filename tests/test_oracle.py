@@ -242,6 +242,19 @@ def test_householder_composition(golden):
     assert O.qr_first_k_columns(A(c["storage"]), np.array(c["tau"]), 0).shape == (3, 0)
 
 
+def test_qt_left_multiply_inverts_q():
+    """Q^T (Q X) = X for the oracle's two reflector orders, and Q^T X equals the
+    least-squares composition's q1^T X (first_k_columns, transposed, times X)."""
+    rng = np.random.default_rng(8)
+    for m, n in ((7, 4), (9, 9), (5, 8)):
+        qr, tau = O.qr_decompose(rng.standard_normal((m, n)))
+        x = rng.standard_normal((m, 3))
+        back = O.qr_qt_left_multiply(qr, tau, O.qr_q_left_multiply(qr, tau, x))
+        assert np.max(np.abs(back - x)) <= 1e-14 * m
+        q = O.qr_first_k_columns(qr, tau, m)
+        assert np.max(np.abs(O.qr_qt_left_multiply(qr, tau, x) - q.T @ x)) <= 1e-14 * m
+
+
 @pytest.mark.parametrize("name,dtype", [("gemm_f32_3x2_2x3", np.float32), ("gemm_f64_3x2_2x3", np.float64)])
 def test_gemm_golden(golden, name, dtype):
     c = golden[name]
