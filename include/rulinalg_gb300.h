@@ -78,6 +78,8 @@ RL_API uint64_t rl_launch_count(void);
 #define RL_TUNE_BATCH_WARP_COST 4     /* systems of cost n^3 (x2 for LU) up to this take the one-warp path in
                                          a largest-first batch: [0, 32768], default 32768 */
 #define RL_TUNE_UPLOAD_CHUNKS 5       /* chunks of the host path's overlapped upload: [1, 256], default 32 */
+#define RL_TUNE_MIXED_REFINE_STEPS 6   /* single-system mixed solves: iterative-refinement steps before
+                                         GMRES-IR takes over: [1, 30], default 30 (LAPACK dsgesv's limit) */
 #define RL_TUNE_TEST_WITHHOLD_CHUNK 100 /* tests only: the host batched path never sets this chunk's arrival
                                            flag, so its wait runs out (RL_ERR_TIMEOUT): [-1, 255], default -1 */
 #define RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK 101 /* tests only: the few-right-hand-side triangular sweep never
@@ -135,7 +137,10 @@ RL_API rl_status rl_dfull_lu_decompose(size_t n, double *a, size_t lda, uint64_t
 /* FullPivLu::solve (lu.rs:480-486) for nrhs right-hand sides: B (n x nrhs, row stride
  * ldb) is overwritten by X = Q U^-1 L^-1 P B; |u_ii| < epsilon returns RL_ERR_DIV_BY_ZERO
  * (back_substitution, src/matrix/mod.rs:333-336), an invalid p or q
- * RL_ERR_INVALID_PERMUTATION. */
+ * RL_ERR_INVALID_PERMUTATION. One deliberate difference: the reference applies q by
+ * scatter (x[q[i]] = y[i], `&self.q * x` at lu.rs:485), which solves A x = b only when q
+ * is its own inverse; this applies it by gather (x[i] = y[q[i]]), the solution for the
+ * factorisation A = (L U)[p][:, q] that the reference's own tests reconstruct. */
 RL_API rl_status rl_sfull_lu_solve(size_t n, size_t nrhs, const float *lu, size_t lda, const uint64_t *p,
                                    const uint64_t *q, float *b, size_t ldb);
 RL_API rl_status rl_dfull_lu_solve(size_t n, size_t nrhs, const double *lu, size_t lda, const uint64_t *p,

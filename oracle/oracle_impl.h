@@ -301,9 +301,11 @@ void FN(or_full_lu_decompose)(size_t n, T *a, size_t lda, uint64_t *p_out, uint6
     free(q);
 }
 
-/* FullPivLu::solve (lu.rs:480-486): y = P b (buffer[p[i]] = b[i],
- * permutation_matrix.rs:369-382), unit-lower forward and upper back substitution
- * (DivByZero when |u_ii| < epsilon), x = Q y the same way with q. b is overwritten. */
+/* FullPivLu::solve (lu.rs:480-486) as the reference writes it: y = P b (buffer[p[i]] =
+ * b[i], permutation_matrix.rs:369-382), unit-lower forward and upper back substitution
+ * (DivByZero when |u_ii| < epsilon), then `&self.q * x` the same way with q
+ * (b[q[i]] = y[i]). That last scatter solves A x = b only when q is its own inverse; the
+ * tests compare the GPU (which gathers, b[i] = y[q[i]]) with the corrected composition. */
 int FN(or_full_lu_solve)(size_t n, const T *lu, size_t lda, const uint64_t *p, const uint64_t *q, T *b) {
     T *y = (T *)malloc(((n) + 1) * sizeof(T));
     for (size_t i = 0; i < n; i++) y[p[i]] = b[i];

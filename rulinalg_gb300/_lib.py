@@ -158,6 +158,7 @@ TUNE_PANEL_CLUSTER_MAX = 2
 TUNE_BATCH_CTAS_PER_SM = 3
 TUNE_BATCH_WARP_COST = 4
 TUNE_UPLOAD_CHUNKS = 5
+TUNE_MIXED_REFINE_STEPS = 6
 TUNE_TEST_WITHHOLD_CHUNK = 100
 TUNE_TEST_WITHHOLD_SWEEP_BLOCK = 101
 

@@ -542,19 +542,17 @@ rl_status diag_inverse(const TA *A, long long lda, int n, int mode, T *Dinv, int
 }
 
 // op(A) Y = Y' for at most kSweepRhs right-hand sides in one sweep launch whose block
-// solves are products with the diagonal blocks' inverses Dinv (diag_inverse). More
-// right-hand sides, or a GPU shared with other streams of this library (the serving
-// workers, see tri_solve_dev), take tri_solve_dev's substitution paths instead.
+// solves are products with the diagonal blocks' inverses Dinv (diag_inverse). ctl:
+// 1 + ceil(n / 64) zeroed ints (the sweep's ticket and block flags). More right-hand
+// sides, or a GPU shared with other streams of this library (the serving workers, see
+// tri_solve_dev), take tri_solve_dev's substitution paths instead.
 template <class T, class TA>
 rl_status tri_solve_inv_dev(const TA *A, long long lda, int n, const T *Dinv, T *Y, long long ldy, int nrhs, int mode,
-                            int *dstatus, cudaStream_t s, T tiny) {
+                            int *dstatus, cudaStream_t s, T tiny, int *ctl) {
     if (nrhs > kSweepRhs || g_shared_gpu) return tri_solve_dev<T, TA>(A, lda, n, Y, ldy, nrhs, mode, dstatus, s, tiny);
     if (n <= 0 || nrhs <= 0) return RL_OK;
     const int nb = ceil_div(n, kSweepRows);
-    DevBuf<int> ctl;
-    RL_TRY(ctl.alloc(1 + nb, s));
-    RL_TRY_CUDA(cudaMemsetAsync(ctl.p, 0, sizeof(int) * (1 + nb), s));
-    RL_LAUNCH((trsv_sweep_kernel<T, TA>), std::min(nb, kSweepCtas), 256, 0, s, A, lda, n, Y, ldy, nrhs, mode, ctl.p,
+    RL_LAUNCH((trsv_sweep_kernel<T, TA>), std::min(nb, kSweepCtas), 256, 0, s, A, lda, n, Y, ldy, nrhs, mode, ctl,
               dstatus, tiny, wait_ns(), (int)tune(RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK), Dinv);
     return RL_OK;
 }

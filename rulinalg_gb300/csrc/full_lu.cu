@@ -262,7 +262,11 @@ rl_status full_lu_decompose_host(size_t n, T *a, size_t lda, uint64_t *p, uint64
 }
 
 // x = Q U^-1 L^-1 P b per column (lu.rs:480-486): permute (y[p[i]] = b[i]), unit-lower
-// and upper solves (DivByZero for |u_ii| < epsilon), then x[q[i]] = y[i].
+// and upper solves (DivByZero for |u_ii| < epsilon), then x[i] = y[q[i]]. The last step
+// deliberately differs from the reference, which writes x[q[i]] = y[i] (`&self.q * x`,
+// lu.rs:485): with A = (L U)[p][:, q] (the reconstruction of lu.rs:903-907) the solution
+// is the gather, and the scatter agrees with it only when q is its own inverse (as in
+// the reference's 4 x 4 tests); otherwise the reference returns a wrong x.
 template <class T>
 rl_status full_lu_solve_host(size_t n, size_t nrhs, const T *lu, size_t lda, const uint64_t *p, const uint64_t *q,
                              T *b, size_t ldb) {
@@ -270,6 +274,8 @@ rl_status full_lu_solve_host(size_t n, size_t nrhs, const T *lu, size_t lda, con
     if (!lu || !p || !q || !b || lda < n || ldb < nrhs || n > (size_t)INT32_MAX || nrhs > (size_t)INT32_MAX)
         return RL_ERR_INVALID_ARG;
     if (!valid_perm(n, p) || !valid_perm(n, q)) return RL_ERR_INVALID_PERMUTATION;
+    std::vector<uint64_t> qinv(n);  // x[i] = y[q[i]] is the scatter x[qinv[j]] = y[j]
+    for (size_t i = 0; i < n; i++) qinv[q[i]] = i;
     RL_TRY(ensure_device());
     cudaStream_t s = cudaStreamPerThread;
     DevBuf<T> dF, dB, dY;
@@ -285,7 +291,7 @@ rl_status full_lu_solve_host(size_t n, size_t nrhs, const T *lu, size_t lda, con
     RL_TRY(copy_h2d(dF.p, n, lu, lda, n, n, s));
     RL_TRY(copy_h2d(dB.p, nrhs, b, ldb, n, nrhs, s));
     RL_TRY_CUDA(cudaMemcpyAsync(dp.p, p, n * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
-    RL_TRY_CUDA(cudaMemcpyAsync(dq.p, q, n * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+    RL_TRY_CUDA(cudaMemcpyAsync(dq.p, qinv.data(), n * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
     const long long tot = (long long)n * nrhs;
     const int g = (int)((tot + 255) / 256);  // one thread per element
     RL_LAUNCH(permute_rows_kernel<T>, g, 256, 0, s, dB.p, (long long)nrhs, dY.p, (long long)nrhs, (int)n, (int)nrhs,

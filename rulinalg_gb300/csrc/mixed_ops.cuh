@@ -99,12 +99,14 @@ struct Minv {
     const int *ipiv;
     int *dstatus;
     DevBuf<double> D1, D2;
+    DevBuf<int> ctl;  // the two sweeps' ticket and block flags
     int mode1() const { return kind == RL_KIND_LU ? 0 : 1; }
     int mode2() const { return kind == RL_KIND_LU ? 2 : 3; }
     rl_status init(cudaStream_t s) {
         const size_t blocks = (size_t)ceil_div(n, kSweepRows) * kSweepRows * kSweepRows;
         RL_TRY(D1.alloc(blocks, s));
         RL_TRY(D2.alloc(blocks, s));
+        RL_TRY(ctl.alloc(2 * (size_t)(1 + ceil_div(n, kSweepRows)), s));
         RL_TRY((diag_inverse<double, float>(F, n, n, mode1(), D1.p, dstatus, s, FLT_MIN)));
         return diag_inverse<double, float>(F, n, n, mode2(), D2.p, dstatus, s, FLT_MIN);
     }
@@ -112,8 +114,10 @@ struct Minv {
         RL_TRY_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
         const double tiny = FLT_MIN;
         if (kind == RL_KIND_LU) RL_TRY(laswp<double>(dst, 1, 1, 0, 0, ipiv, 0, n, s));
-        RL_TRY((tri_solve_inv_dev<double, float>(F, n, n, D1.p, dst, 1, 1, mode1(), dstatus, s, tiny)));
-        return tri_solve_inv_dev<double, float>(F, n, n, D2.p, dst, 1, 1, mode2(), dstatus, s, tiny);
+        const int words = 1 + ceil_div(n, kSweepRows);
+        RL_TRY_CUDA(cudaMemsetAsync(ctl.p, 0, 2 * words * sizeof(int), s));
+        RL_TRY((tri_solve_inv_dev<double, float>(F, n, n, D1.p, dst, 1, 1, mode1(), dstatus, s, tiny, ctl.p)));
+        return tri_solve_inv_dev<double, float>(F, n, n, D2.p, dst, 1, 1, mode2(), dstatus, s, tiny, ctl.p + words);
     }
 };
 
@@ -419,7 +423,8 @@ struct MixedFactor {
         RL_TRY_CUDA(cudaMemset2DAsync(X, ldx * sizeof(double), 0, nrhs * sizeof(double), n, s));
         RL_LAUNCH(update_x_kernel, ge, 256, 0, s, X, ldx, W.p, (long long)nrhs, n, nrhs, bn_b, active.p);
         std::vector<unsigned long long> hb(3 * nrhs);
-        bool stalled = false, need_fp64 = false;
+        bool stalled = false, need_fp64 = false, diverged = false;
+        const int max_steps = (int)tune(RL_TUNE_MIXED_REFINE_STEPS);
         for (int it = 0;; it++) {
             RL_TRY(residual_dev(A, lda, n, X, ldx, B, ldb, R.p, nrhs, nrhs, s));
             RL_TRY(colnorm_dev(R.p, nrhs, n, nrhs, rn_b, s));
@@ -441,9 +446,14 @@ struct MixedFactor {
                 const double den = anorm * xn + bnorm[c];
                 berr = std::max(berr, den > 0 ? rn / den : 0.0);
                 near[c] = rn <= 10.0 * n * kU * den;
-                // diverging (a growing residual) or stalling (not halving after two steps)
-                if (!conv[c] && ((it >= 1 && rn > prev[c]) || (it >= 2 && rn > 0.5 * prev[c]))) stalled = true;
-                if (!std::isfinite(rn)) stalled = true;
+                // Stalling: less than 10% progress in a step. Slow but steady refinement
+                // (kappa u_32 ~ 0.5, a step costs a GEMV and two triangular solves) is
+                // cheaper to finish than an FP64 refactor; LAPACK dsgesv allows 30 steps.
+                if (!conv[c] && it >= 1 && rn > 0.9 * prev[c]) stalled = true;
+                // Diverging: the first correction made the residual grow (kappa u_32 > 1):
+                // the FP32 factor is too far off for GMRES-IR to pay off against the refactor.
+                if (!conv[c] && it == 1 && rn > prev[c]) diverged = true;
+                if (!std::isfinite(rn)) stalled = diverged = true;
                 prev[c] = rn;
                 all &= conv[c];
                 act[c] = !conv[c];
@@ -453,7 +463,7 @@ struct MixedFactor {
             // LAPACK dsgesv's test and step limit (30); a column that stalls or runs out
             // of steps is accepted within the 10 n u backward-error bound (the batched
             // solver's rule), where a large n's residual floor can sit above the test
-            if (all || stalled || it >= 30) {
+            if (all || stalled || it >= max_steps) {
                 for (int c = 0; c < nrhs; c++) conv[c] |= near[c];
                 break;
             }
@@ -466,6 +476,7 @@ struct MixedFactor {
             bool all_ok = true;
             for (int c = 0; c < nrhs; c++) all_ok &= conv[c] != 0;
             if (all_ok) return RL_OK;
+            need_fp64 = diverged;
         }
         if (!need_fp64) {
             // GMRES-IR on each remaining column, within a budget of the estimated time of
@@ -481,7 +492,7 @@ struct MixedFactor {
             DevBuf<double> xb, bb;
             RL_TRY(xb.alloc(n, s));
             RL_TRY(bb.alloc(n, s));
-            Minv M{F, n, kind, ipiv, dstatus.p + 1, {}, {}};
+            Minv M{F, n, kind, ipiv, dstatus.p + 1, {}, {}, {}};
             RL_TRY(M.init(s));
             for (int c = 0; c < nrhs && !need_fp64; c++) {
                 if (conv[c]) continue;

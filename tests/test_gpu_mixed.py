@@ -104,3 +104,30 @@ def test_lstsq_mixed_ill_conditioned_falls_back(gpu):
     x, info = gpu.lstsq_mixed(a, b)
     assert info["path"] == "fp64", info
     assert np.max(np.abs(x - x_true)) <= 1e-5 * np.max(np.abs(x_true)), info
+
+
+def test_gmres_ir_taken_and_converges(gpu):
+    """GMRES-IR itself: with iterative refinement held to one step
+    (RL_TUNE_MIXED_REFINE_STEPS = 1) a kappa = 1e6 system, which refinement would finish
+    in several steps, goes on to GMRES-IR (restarted FP64 GMRES with the FP32 factor
+    applied in FP64 through inverted diagonal blocks). The path is gmres-ir, GMRES
+    converges inside its budget, and the solution is f64-accurate and within the
+    kappa-scaled forward-error bound of the FP64 oracle's solution."""
+    from rulinalg_gb300 import _lib as L
+    from rulinalg_gb300.workloads import conditioned_system
+    n, kappa = 2048, 1e6
+    a, b = conditioned_system(n, kappa, 1, seed=2048 + 6)
+    b = b[:, 0]
+    gpu.tune_set(L.TUNE_MIXED_REFINE_STEPS, 1)
+    try:
+        x, info = gpu.solve_mixed(a, b, "lu")
+    finally:
+        gpu.tune_set(L.TUNE_MIXED_REFINE_STEPS, 30)
+    assert info["path"] == "gmres-ir" and info["gmres_iters"] > 0, info
+    assert backward_error(a, x, b) <= n * U64 * 10
+    lu, perm, st = O.lu_decompose(a, threads=8)
+    xo, _ = O.lu_solve(lu, perm, b)
+    eta = lambda v: np.linalg.norm(b - a @ v) / (np.linalg.norm(v) + np.linalg.norm(b))
+    fe = np.linalg.norm(x - xo) / np.linalg.norm(xo)
+    assert fe <= 2 * kappa * (eta(x) + eta(xo)), (fe, info)
+    print(f"GMRES-IR n={n} kappa={kappa:.0e}: {info}, forward error vs oracle {fe:.2e}")

@@ -325,3 +325,49 @@ def test_batch_loop_matches_single_calls():
             lu, perm, _ = O.lu_decompose(m)
             want, _ = O.lu_solve(lu, perm, r)
         assert np.array_equal(b[b_off[i]:b_off[i] + ns[i]], want)
+
+
+def _corrected_full_lu_solve(olu, op, oq, b):
+    y, st = O.full_lu_solve(olu, op, np.arange(len(oq), dtype=np.uint64), b)
+    return y[oq.astype(np.int64)], st
+
+
+def test_full_lu_reference_solve_scatter_differs_only_for_non_involutions():
+    """The reference's FullPivLu::solve applies q by scatter (`&self.q * x`, lu.rs:485): on
+    its own 4 x 4 case that agrees with the gather x[i] = y[q[i]]; on a random 40 x 40
+    matrix the scatter's x does not solve A x = b and the gather's is f64-accurate (the
+    GPU path gathers)."""
+    from comparators import backward_error
+    a = np.array([[5.0, 0, 0, 1], [2, 2, 2, 1], [4, 5, 5, 5], [1, 6, 4, 5]])
+    b = np.array([9.0, 16, 49, 45])
+    olu, op, oq, _, _ = O.full_lu_decompose(a)
+    assert np.array_equal(O.full_lu_solve(olu, op, oq, b)[0], _corrected_full_lu_solve(olu, op, oq, b)[0])
+    rng = np.random.default_rng(40)
+    a = rng.uniform(-1, 1, (40, 40))
+    b = rng.standard_normal(40)
+    olu, op, oq, _, _ = O.full_lu_decompose(a)
+    assert backward_error(a, O.full_lu_solve(olu, op, oq, b)[0], b) > 1e-3
+    assert backward_error(a, _corrected_full_lu_solve(olu, op, oq, b)[0], b) <= 40 * 2.0 ** -53 * 10
+
+
+def test_full_lu_oracle_golden(golden):
+    """FullPivLu restatement against the reference's known answers (lu.rs:892-1018, the
+    rank doc example lu.rs:537-541): reconstruction (L U)[p][:, q] = A, ranks, the 4 x 4
+    solve within 100 ULP, the inverse, and a singular matrix that is not invertible."""
+    for name in ("full_lu_reconstruct_4x4", "full_lu_singular_rank3", "full_lu_doc_rank2"):
+        c = golden[name]
+        a = A(c["a"])
+        lu, p, q, _, _ = O.full_lu_decompose(a)
+        n = len(a)
+        rec = ((np.tril(lu, -1) + np.eye(n)) @ np.triu(lu))[p.astype(np.int64)][:, q.astype(np.int64)]
+        assert_matrix_float_eq(rec, a)
+        if "rank" in c:
+            assert O.full_lu_rank(lu) == c["rank"]
+    c = golden["full_lu_solve_4x4"]
+    lu, p, q, _, _ = O.full_lu_decompose(A(c["a"]))
+    x, st = O.full_lu_solve(lu, p, q, np.array(c["b"]))
+    assert st == O.OK
+    assert_ulp_eq(x, np.array(c["x"]), c["ulp_tol"])
+    c = golden["full_lu_noninvertible_3x3"]
+    lu, _, _, _, _ = O.full_lu_decompose(A(c["a"]))
+    assert not O.full_lu_is_invertible(lu)
