@@ -60,6 +60,9 @@ def parse():
     p.add_argument("--sizes", default="", help="comma-separated sizes for dense / mixed")
     p.add_argument("--kappas", default="1e2,1e6,1e10", help="mixed: condition numbers")
     p.add_argument("--nrhs", default="1,64", help="mixed: right-hand-side counts")
+    p.add_argument("--gen", default="haar", choices=["haar", "uniform"],
+                   help="mixed: A = U diag(sigma) V^T (haar) or U(-1,1) + n/2 I (uniform, no factorisation "
+                        "needed to build it; kappa is then ignored)")
     p.add_argument("--lambdas", default="1000,10000,50000", help="serve: arrival rates (requests/s)")
     p.add_argument("--serve-seconds", type=float, default=60.0, help="serve: stream length per rate")
     return p.parse_args()
@@ -336,7 +339,7 @@ def config2(dev, sizes=(1024, 2048, 4096, 8192), steps=3, warm=3):
             "l2": "256 MB buffer overwritten before every timed call"}
 
 
-def config3(dev, sizes=(4096, 8192, 16384), kappas=(1e2, 1e6, 1e10), nrhs_list=(1, 64)):
+def config3(dev, sizes=(4096, 8192, 16384), kappas=(1e2, 1e6, 1e10), nrhs_list=(1, 64), gen="haar"):
     """Mixed-precision single-system LU solves (FP32 factor, FP64 refinement, GMRES-IR,
     FP64 refactor) against the plain FP64 GPU solve: A = U diag(sigma) V^T, Haar U, V,
     sigma geometric from 1 to 1/kappa, 1 and 64 N(0,1) right-hand sides. Forward error of
@@ -354,9 +357,16 @@ def config3(dev, sizes=(4096, 8192, 16384), kappas=(1e2, 1e6, 1e10), nrhs_list=(
     for n in sizes:
         reps = 3 if n <= 8192 else 1
         for kappa in kappas:
-            a, bfull = conditioned_system(n, kappa, 64, seed=n + int(np.log10(kappa)), device=dev)
+            if gen == "haar":
+                a, bfull = conditioned_system(n, kappa, 64, seed=n + int(np.log10(kappa)), device=dev)
+            else:
+                g = torch.Generator(device=dev)
+                g.manual_seed(n)
+                a = torch.rand(n, n, dtype=torch.float64, device=dev, generator=g) * 2 - 1
+                a += torch.eye(n, dtype=torch.float64, device=dev) * (n / 2)
+                bfull = torch.randn(n, 64, dtype=torch.float64, device=dev, generator=g)
             xo_all = None
-            if n == 4096 and 64 in nrhs_list:
+            if n == 4096 and 64 in nrhs_list and gen == "haar":
                 import oracle as O
                 ah, bh = a.cpu().numpy(), bfull.cpu().numpy()
                 lu, perm, st = O.lu_decompose(ah, threads=os.cpu_count() or 1)
@@ -532,7 +542,7 @@ def main():
                 out = config2(dev, sizes or (1024, 2048, 4096, 8192))
             elif args.workload == "mixed":
                 out = config3(dev, sizes or (4096, 8192, 16384), tuple(float(v) for v in args.kappas.split(",")),
-                              tuple(int(v) for v in args.nrhs.split(",")))
+                              tuple(int(v) for v in args.nrhs.split(",")), args.gen)
             else:
                 out = config5(dev, args)
         out["clocks"] = clk.summary()
