@@ -112,6 +112,7 @@ rl_status record(rl_batch_plan *p, const TI *a, const TI *b, TI *x, int *info, i
 template <class TI, class TF, bool MIXED>
 rl_status run_plan(rl_batch_plan *p, const TI *a, const TI *b, TI *x, int *info, int *iters, double *berr,
                    cudaStream_t s) {
+    NvtxRange nvtx_("rl.batch.solve_dev");
     const void *key[6] = {a, b, x, info, iters, berr};
     if (!p->exec || !std::equal(key, key + 6, p->key)) {
         if (p->exec) {
@@ -202,6 +203,7 @@ rl_status launch_gated(rl_batch_plan *p, const TI *a, const TI *b, TI *x, cudaSt
 template <class TI>
 rl_status solve_host(rl_batch_plan *p, const TI *a, const TI *b, TI *x, int32_t *info, int32_t *iters,
                      double *berr) {
+    NvtxRange nvtx_("rl.batch.solve_host");
     cudaStream_t s = cudaStreamPerThread;
     if (p->count == 0) return RL_OK;
     if (!p->h_a) {

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <atomic>
 #include <cstddef>
@@ -91,6 +92,16 @@ inline rl_status copy_d2h(T *dst, size_t ldd, const T *src, size_t lds, size_t r
                                   cudaMemcpyDeviceToHost, s));
     return RL_OK;
 }
+
+// A named NVTX range around a phase of the library's work (a factorisation, a refinement
+// loop, a batched solve): profilers attached to the process (ncu --nvtx, nsys) show and
+// filter by it; without one the calls return at once.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 template <class T>
 struct Eps;

@@ -22,6 +22,7 @@ namespace {
 template <class T>
 rl_status gemm_public(int m, int n, int k, const T *a, long long lda, const T *b, long long ldb, T *c, long long ldc,
                       cudaStream_t s, bool &used_tc) {
+    NvtxRange nvtx_("rl.gemm");
     used_tc = false;
     if constexpr (std::is_same<T, float>::value) used_tc = sgemm_tc_eligible(m, n, k);
     return gemm<T, false, false>(m, n, k, T(1), a, lda, b, ldb, T(0), c, ldc, s);

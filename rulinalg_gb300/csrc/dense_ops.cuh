@@ -191,6 +191,7 @@ constexpr int outer_nb() {
 // partial pivoting over the whole column either way.
 template <class T>
 rl_status lu_factor_dev(T *A, long long lda, int n, int *ipiv, cudaStream_t s, T tiny = Eps<T>::value) {
+    NvtxRange nvtx_("rl.lu.factor");
     if (n <= 0) return RL_OK;
     if (n <= CTA_NMAX) return factor_small<T>(A, lda, n, 0, ipiv, s, tiny);
     constexpr int NB = PanelNB<T>::value;
@@ -264,6 +265,7 @@ rl_status lu_factor_dev(T *A, long long lda, int n, int *ipiv, cudaStream_t s, T
 // strict upper triangle is never written either way.
 template <class T>
 rl_status chol_factor_dev(T *A, long long lda, int n, cudaStream_t s, T tiny = Eps<T>::value) {
+    NvtxRange nvtx_("rl.cholesky.factor");
     if (n <= 0) return RL_OK;
     if (n <= CTA_NMAX) return factor_small<T>(A, lda, n, 1, nullptr, s, tiny);
     if constexpr (outer_nb<T>() > 0) {
@@ -323,6 +325,7 @@ rl_status block_t_factor(const T *V, int mrows, int kb, const T *tau, T *part, i
 // (min(m, n) for a plain QR; n for the augmented least-squares matrix).
 template <class T>
 rl_status qr_factor_dev(T *A, long long lda, int m, int n, int nrefl, T *tau, cudaStream_t s) {
+    NvtxRange nvtx_("rl.qr.factor");
     if (nrefl <= 0) return RL_OK;
     constexpr int NB = PanelNB<T>::value;
     int Gmax, rp;

@@ -186,6 +186,7 @@ __global__ void __launch_bounds__(kFpThreads) full_piv_lu_kernel(T *A, long long
 // pivot). Synchronises the stream.
 template <class T>
 rl_status full_lu_dev(T *A, long long lda, int n, int *piv_r, int *piv_c, int &steps, cudaStream_t s) {
+    NvtxRange nvtx_("rl.full_lu.factor");
     steps = 0;
     if (n <= 0) return RL_OK;
     auto kern = full_piv_lu_kernel<T>;

@@ -145,6 +145,7 @@ inline double host_seconds() {
 
 inline rl_status gmres_ir(const double *A, long long lda, int n, const Minv &M, const double *b, double *x, double anorm,
                    double bnorm, double deadline, SolveOut &out, bool &ok, cudaStream_t s) {
+    NvtxRange nvtx_("rl.mixed.gmres_ir");
     constexpr int m = 64, outer_max = 5;
     const double inner_tol = 1e-8;
     DevBuf<double> V, H, cs, sn, g, y, w, r, t, nrm2, partial;
@@ -328,6 +329,7 @@ struct MixedFactor {
     // own = true copies A into the factor (resident factors outlive the caller's buffer);
     // adopt = true takes ownership of `a` itself (a device buffer from cudaMallocAsync).
     rl_status factor(const double *a, long long lda_, int n_, int kind_, bool own, cudaStream_t s, bool adopt = false) {
+        NvtxRange nvtx_("rl.mixed.factor_fp32");
         n = n_;
         kind = kind_;
         home = s;
@@ -377,6 +379,7 @@ struct MixedFactor {
 
     rl_status solve_with_fp64(const double *B, long long ldb, double *X, long long ldx, int nrhs, SolveOut &out,
                               cudaStream_t s) {
+        NvtxRange nvtx_("rl.mixed.fp64_refactor_solve");
         out.path = RL_PATH_FP64;
         RL_TRY(ensure_fp64(s));
         DevBuf<int> st;
@@ -397,6 +400,7 @@ struct MixedFactor {
     }
 
     rl_status solve(const double *B, long long ldb, double *X, long long ldx, int nrhs, SolveOut &out, cudaStream_t s) {
+        NvtxRange nvtx_("rl.mixed.refine");
         out = SolveOut();
         if (!f32_ok) return solve_with_fp64(B, ldb, X, ldx, nrhs, out, s);
         DevBuf<float> W;
@@ -578,6 +582,7 @@ struct GemvT {
 // inf-norms, for the returned x.
 inline rl_status lstsq_mixed(const double *A, long long lda, int m, int n, const double *b, double *x, SolveOut &out,
                              cudaStream_t s) {
+    NvtxRange nvtx_("rl.mixed.lstsq");
     out = SolveOut();
     if (m < n) return RL_ERR_SHAPE;
     if (n == 0) return RL_OK;

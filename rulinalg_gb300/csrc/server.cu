@@ -158,6 +158,7 @@ struct Worker {
 
     // Several small systems in one batched mixed-precision launch.
     rl_status run_batch(std::vector<Req *> &job) {
+        NvtxRange nvtx_("rl.server.batch");
         cudaStream_t st = stream;
         const int B = (int)job.size();
         std::vector<int> n(B), order(B);
@@ -299,6 +300,7 @@ struct Worker {
     }
 
     rl_status run_resolve(Req *q) {
+        NvtxRange nvtx_("rl.server.resolve");
         std::shared_ptr<Resident> res;
         {
             std::lock_guard<std::mutex> lk(s->mu);
@@ -317,6 +319,7 @@ struct Worker {
     // min ||A x - b|| (m >= n) through the mixed-precision least-squares solver (FP32
     // QR, FP64 semi-normal-equation refinement, FP64 QR fallback).
     rl_status run_lstsq(Req *q) {
+        NvtxRange nvtx_("rl.server.lstsq");
         cudaStream_t st = stream;
         const rl_request &r = q->r;
         const int m = (int)r.m, n = (int)r.n;
