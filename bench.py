@@ -50,10 +50,11 @@ def parse():
                    help="CPU baseline sample size in GFLOP of factorisation work")
     p.add_argument("--skip-e2e", action="store_true")
     p.add_argument("--skip-cpu", action="store_true")
-    p.add_argument("--workload", default="batch", choices=["batch", "dense", "mixed", "serve"],
+    p.add_argument("--workload", default="batch", choices=["batch", "dense", "mixed", "serve", "factors"],
                    help="batch (default): the headline batched mix, followed by the other configurations as "
                         "sub-objects of the same line; dense / mixed / serve: only that configuration, as its "
-                        "own line (GEMM sweep + FP64 LU; single-system mixed precision; served stream)")
+                        "own line (GEMM sweep + FP64 LU; single-system mixed precision; served stream; "
+                        "single factorisations: LU, Cholesky, QR, FullPivLu)")
     p.add_argument("--configs", default="1,2,3,4f,5",
                    help="configurations reported beside the headline: 1 (LU n=1024), 2 (GEMM sweep, FP64 LU), "
                         "3 (mixed single systems), 4f (f32 SPD half of the batch), 5 (served stream); '' for none")
@@ -399,6 +400,47 @@ def config3(dev, sizes=(4096, 8192, 16384), kappas=(1e2, 1e6, 1e10), nrhs_list=(
             "all_within": all(c["mixed"]["within"] for c in cases), "cases": cases}
 
 
+def factors(n: int = 4096, reps: int = 3):
+    """Single factorisations through the host-pointer entry points (each call copies A in
+    and the factor out): PartialPivLu and Cholesky in f32 and f64, Householder QR of an
+    n x n and of a 2n x n matrix in f32 and f64, FullPivLu in f64. Median wall time of
+    `reps` calls after one warm-up; GFLOP/s on the reference's flop counts (LU 2/3 n^3,
+    Cholesky 1/3 n^3, QR 2 m n^2 - 2/3 n^3), and for FullPivLu the bytes its passes move
+    (each step reads and writes the trailing block: about n^3/3 elements each way)."""
+    import rulinalg_gb300 as rl
+    rng = np.random.default_rng(n)
+    g = rng.standard_normal((n, n))
+    spd = g @ g.T / n + np.eye(n)
+    gen = rng.uniform(-1, 1, (n, n)) + np.eye(n)
+    tall = rng.standard_normal((2 * n, n))
+    out = {"workload": f"single factorisations, n = {n} (QR also 2n x n)", "n": n, "runs": []}
+
+    def timed(name, fn, flops=None, bytes_moved=None):
+        fn()
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            ts.append(time.perf_counter() - t0)
+        ms = 1e3 * statistics.median(ts)
+        row = {"op": name, "ms_host_api": ms}
+        if flops:
+            row["gflops"] = flops / (ms / 1e3) / 1e9
+        if bytes_moved:
+            row["gbs"] = bytes_moved / (ms / 1e3) / 1e9
+        out["runs"].append(row)
+
+    for dt in (np.float32, np.float64):
+        tag = "f32" if dt == np.float32 else "f64"
+        timed(f"lu_{tag}", lambda: rl.PartialPivLu.decompose(gen.astype(dt)), 2.0 * n ** 3 / 3)
+        timed(f"cholesky_{tag}", lambda: rl.Cholesky.decompose(spd.astype(dt)), n ** 3 / 3.0)
+        timed(f"qr_{tag}", lambda: rl.HouseholderQr.decompose(gen.astype(dt)), 4.0 * n ** 3 / 3)
+        timed(f"qr_tall_{tag}", lambda: rl.HouseholderQr.decompose(tall.astype(dt)),
+              2.0 * 2 * n * n * n - 2.0 * n ** 3 / 3)
+    timed("full_piv_lu_f64", lambda: rl.FullPivLu.decompose(gen), 2.0 * n ** 3 / 3, 2 * 8 * n ** 3 / 3.0)
+    return out
+
+
 def config4_f32(dev, args):
     """The f32 half of the SPD set: 20,000 Cholesky systems as Matrix<f32> (FP32 plan,
     graph-captured, device pointers)."""
@@ -540,6 +582,8 @@ def main():
         with ClockSampler(local) as clk:
             if args.workload == "dense":
                 out = config2(dev, sizes or (1024, 2048, 4096, 8192))
+            elif args.workload == "factors":
+                out = factors(sizes[0] if sizes else 4096)
             elif args.workload == "mixed":
                 out = config3(dev, sizes or (4096, 8192, 16384), tuple(float(v) for v in args.kappas.split(",")),
                               tuple(int(v) for v in args.nrhs.split(",")), args.gen)
