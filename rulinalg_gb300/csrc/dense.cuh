@@ -862,9 +862,11 @@ static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const TA *__rest
             }
             __syncthreads();
             if (s_fail) break;
-            for (int idx = tid; idx < ks * nrhs; idx += blockDim.x) {
+            // rows ks..BR-1 of a short last block are zeroed: they meet a[jj] = 0, and a
+            // stale shared value there could be a NaN (0 * NaN = NaN)
+            for (int idx = tid; idx < BR * nrhs; idx += blockDim.x) {
                 const int i = idx / nrhs, c = idx - i * nrhs;
-                xs[i * kSweepRhs + c] = __ldcg(Y + (long long)(c0 + i) * ldy + c);
+                xs[i * kSweepRhs + c] = i < ks ? __ldcg(Y + (long long)(c0 + i) * ldy + c) : T(0);
             }
             __syncthreads();
     #pragma unroll

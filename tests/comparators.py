@@ -59,7 +59,10 @@ def perm_from_matrix(p):
 
 def backward_error(a, x, b):
     """Normwise backward error ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf),
-    evaluated in extended precision on the test side."""
+    evaluated in extended precision on the test side; a non-finite x or b gives inf
+    (a longdouble max reduction need not propagate NaN on every platform)."""
+    if not (np.all(np.isfinite(x)) and np.all(np.isfinite(b))):
+        return float("inf")
     a = np.asarray(a, dtype=np.longdouble)
     x = np.asarray(x, dtype=np.longdouble)
     b = np.asarray(b, dtype=np.longdouble)

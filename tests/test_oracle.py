@@ -371,3 +371,13 @@ def test_full_lu_oracle_golden(golden):
     c = golden["full_lu_noninvertible_3x3"]
     lu, _, _, _, _ = O.full_lu_decompose(A(c["a"]))
     assert not O.full_lu_is_invertible(lu)
+
+
+def test_backward_error_flags_non_finite():
+    """The test-side backward error is inf for a solution with a NaN or inf entry, so a
+    NaN produced by a kernel can never pass a backward-error bound."""
+    from comparators import backward_error
+    a = np.eye(3)
+    assert backward_error(a, np.array([np.nan, 1.0, 1.0]), np.ones(3)) == float("inf")
+    assert backward_error(a, np.array([np.inf, 1.0, 1.0]), np.ones(3)) == float("inf")
+    assert backward_error(a, np.ones(3), np.ones(3)) == 0.0
