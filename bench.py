@@ -66,6 +66,8 @@ def parse():
                         "needed to build it; kappa is then ignored)")
     p.add_argument("--lambdas", default="1000,10000,50000", help="serve: arrival rates (requests/s)")
     p.add_argument("--serve-seconds", type=float, default=60.0, help="serve: stream length per rate")
+    p.add_argument("--tune", default="", help="library tunables set before the run: key=value[,key=value] with "
+                                              "the RL_TUNE_* keys of include/rulinalg_gb300.h")
     return p.parse_args()
 
 
@@ -235,6 +237,20 @@ FP64_PEAK_TFLOPS = 1.25  # GB300's FP64 rate (nominal; rl_dgemm_dev sustains it 
 
 def peaks():
     return json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+
+
+def profile_traffic(a_bytes: float, path=None):
+    """DRAM bytes per launch of the batched kernel for a batch of a_bytes matrix bytes,
+    from the committed ncu summary's line `traffic_per_launch_bytes: T @ M` (T bytes for
+    a batch of M matrix bytes), scaled by matrix bytes; None without that line."""
+    path = path or ROOT / "profiles" / "batch_solve_kernel_mixed_40k_mix.md"
+    if not Path(path).exists():
+        return None
+    for line in Path(path).read_text().splitlines():
+        if line.startswith("traffic_per_launch_bytes:") and "@" in line:
+            t, m = line.split(":", 1)[1].split("@")
+            return float(t) * a_bytes / float(m)
+    return None
 
 
 def tf32x3_ceiling_tflops():
@@ -577,6 +593,9 @@ def main():
     torch.cuda.set_device(dev)
     if not rl.device_available():
         raise SystemExit("rulinalg_gb300: no usable sm_103 GPU")
+    for kv in filter(None, args.tune.split(",")):
+        k, v = kv.split("=")
+        rl.tune_set(int(k), int(float(v)))
     if args.workload != "batch":
         sizes = tuple(int(v) for v in args.sizes.split(",")) if args.sizes else None
         with ClockSampler(local) as clk:
@@ -702,12 +721,7 @@ def main():
     # DRAM traffic per launch from the committed ncu summary of this kernel (captured on a
     # 6,000-system batch of the same mix and scaled there to 40,000 by matrix bytes);
     # scaled here by matrix bytes to this run's batch.
-    traffic = None
-    prof = ROOT / "profiles" / "batch_solve_kernel_mixed_40k_mix.md"
-    if prof.exists():
-        for line in prof.read_text().splitlines():
-            if line.startswith("traffic_per_launch_bytes:"):
-                traffic = float(line.split(":")[1]) * a_bytes / float(line.split("@")[1]) if "@" in line else None
+    traffic = profile_traffic(a_bytes)
     fp64_peak = FP64_PEAK_TFLOPS
     fp64_floor_ms = fl64 / (fp64_peak * 1e12) * 1e3
     roofline = {"bound": "hbm", "achieved": alg_bytes / t_k / 1e9, "peak": hbm_peak, "unit": "GB/s",
@@ -789,8 +803,14 @@ def main():
                                   ("5", "config5_served_stream", lambda: config5(dev, args))):
                 if key in wanted:
                     t0 = time.perf_counter()
-                    configs[name] = fn()
+                    try:
+                        configs[name] = fn()
+                    except Exception as e:  # reported in the line; the headline stands on its own
+                        import traceback
+                        traceback.print_exc()
+                        configs[name] = {"error": f"{type(e).__name__}: {e}"}
                     configs[name]["wall_s"] = time.perf_counter() - t0
+                    torch.cuda.synchronize()
                     torch.cuda.empty_cache()
         configs["clocks"] = clk.summary()
         line["configs"] = configs

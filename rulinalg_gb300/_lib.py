@@ -159,6 +159,7 @@ TUNE_BATCH_CTAS_PER_SM = 3
 TUNE_BATCH_WARP_COST = 4
 TUNE_UPLOAD_CHUNKS = 5
 TUNE_MIXED_REFINE_STEPS = 6
+TUNE_LU_OUTER_NB = 7
 TUNE_TEST_WITHHOLD_CHUNK = 100
 TUNE_TEST_WITHHOLD_SWEEP_BLOCK = 101
 

@@ -210,7 +210,11 @@ rl_status lu_factor_dev(T *A, long long lda, int n, int *ipiv, cudaStream_t s, T
     // after it runs on in-range indices, and every later panel stops at its first barrier.
     RL_TRY_CUDA(cudaMemsetAsync(sync.p, 0, sizeof(PanelSync), s));
     unsigned long long wns = wait_ns();
-    const int NBO = outer_nb<T>() > 0 ? outer_nb<T>() : n;
+    int NBO = n;  // FP32: outer blocks of RL_TUNE_LU_OUTER_NB columns (a multiple of NB)
+    if constexpr (std::is_same<T, float>::value) {
+        const int w = (int)(tune(RL_TUNE_LU_OUTER_NB) / NB) * NB;
+        if (w >= NB) NBO = w;
+    }
     for (int K0 = 0; K0 < n; K0 += NBO) {
         const int K1 = std::min(n, K0 + NBO), KB = K1 - K0;
         for (int k0 = K0; k0 < K1; k0 += NB) {

@@ -64,3 +64,15 @@ def test_autotune_key_follows_the_size_histogram(rl):
     assert batch_key(n1, k1, 1, "GB300") != batch_key(n1, [1, 0, 1, 1, 0], 1, "GB300")
     assert batch_key(n1, k1, 1, "GB300") != batch_key(n1, k1, 0, "GB300")
     assert batch_key(n1, k1, 1, "GB300") != batch_key(n1, k1, 1, "other")
+
+
+def test_bench_profile_traffic_line(tmp_path):
+    """bench.py scales the committed batched-kernel traffic line `T @ M` by matrix bytes."""
+    import bench
+    p = tmp_path / "prof.md"
+    p.write_text("x\ntraffic_per_launch_bytes: 99200000000 @ 10012700000\n")
+    assert abs(bench.profile_traffic(10012700000, p) - 99.2e9) < 1
+    assert abs(bench.profile_traffic(5006350000, p) - 49.6e9) < 1
+    p.write_text("traffic_per_launch_bytes: 99200000000\n")
+    assert bench.profile_traffic(1.0, p) is None
+    assert bench.profile_traffic(1.0) is not None  # the committed profile carries the line

@@ -164,3 +164,35 @@ def test_poisson_replay(gpu, server):
     st = server.stats()
     assert st["completed"] == count and st["p99_us"] >= st["p50_us"] > 0
     print(f"replay: {st}")
+
+
+def test_backpressure_replay_arrays(gpu):
+    """max_pending = 4: a burst of 200 requests arriving at once through the array replay
+    (the form the served-stream benchmark uses) is partly refused with RL_ERR_BUSY; the
+    refusals are counted in the statistics, and every accepted request completes
+    f64-accurate into its own output buffer."""
+    from rulinalg_gb300._lib import REQUEST_DTYPE
+    rng = np.random.default_rng(7)
+    srv = gpu.Server(workers=2, max_pending=4)
+    try:
+        count = 200
+        systems = [system(rng, 0, int(rng.integers(300, 700))) for _ in range(count)]
+        xs = [np.zeros(len(b)) for _, b in systems]
+        req = np.zeros(count, dtype=REQUEST_DTYPE)
+        req["kind"] = gpu.REQ_LU
+        for i, (a, b) in enumerate(systems):
+            req[i]["m"] = req[i]["n"] = len(b)
+            req[i]["a"], req[i]["b"], req[i]["x"] = a.ctypes.data, b.ctypes.data, xs[i].ctypes.data
+        res = srv.replay_arrays(np.zeros(count), req)
+        busy = res["status"] == 37
+        ok = res["status"] == 0
+        assert busy.any() and ok.sum() >= 4 and (busy | ok).all()
+        assert srv.stats()["rejected"] == busy.sum()
+        for i in np.nonzero(ok)[0]:
+            a, b = systems[i]
+            assert backward_error(a, xs[i], b) <= len(b) * U64 * 10
+            assert res["berr"][i] <= len(b) * U64 * 10
+        for i in np.nonzero(busy)[0]:
+            assert not xs[i].any()
+    finally:
+        srv.close()
