@@ -81,9 +81,10 @@ RL_API uint64_t rl_launch_count(void);
 #define RL_TUNE_MIXED_REFINE_STEPS 6   /* single-system mixed solves: iterative-refinement steps before
                                          GMRES-IR takes over: [1, 30], default 30 (LAPACK dsgesv's limit) */
 #define RL_TUNE_LU_OUTER_NB 7         /* FP32 blocked LU (n > 512): width of the outer column blocks whose
-                                         trailing update is one K = width GEMM on the tensor cores: [0, 4096],
-                                         rounded down to a multiple of 64, default 256; below 64 (e.g. 0):
-                                         one level, every 64-column panel updates the whole trailing matrix */
+                                         trailing update is one K = width GEMM on the tensor cores: [-1, 4096],
+                                         rounded down to a multiple of 64; 0..63: one level, every 64-column
+                                         panel updates the whole trailing matrix; -1 (default): one level for
+                                         n < 6144, 512-column blocks from there (measured best on GB300) */
 #define RL_TUNE_TEST_WITHHOLD_CHUNK 100 /* tests only: the host batched path never sets this chunk's arrival
                                            flag, so its wait runs out (RL_ERR_TIMEOUT): [-1, 255], default -1 */
 #define RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK 101 /* tests only: the few-right-hand-side triangular sweep never

@@ -172,12 +172,12 @@ template <class T, class TA = T>
 rl_status tri_solve_dev(const TA *A, long long lda, int n, T *Y, long long ldy, int nrhs, int mode, int *dstatus,
                         cudaStream_t s, T tiny = Eps<T>::value);
 
-// Outer block width of the blocked factorisations. FP32 (the mixed-precision factor and
+// Outer block width of the blocked Cholesky. FP32 (the mixed-precision factor and
 // Matrix<f32>): 256-column blocks, each factored with the 64-column panels confined to
 // the block, then ONE trailing update of K = 256 on the tensor cores (tcgen05, 3xTF32;
 // the K = 64 updates of the inner panels measured slower there and stay on the SIMT
 // kernel). FP64: 0, one block spanning the matrix (every update is a K = 64 DFMA GEMM,
-// already at the FP64 rate).
+// already at the FP64 rate). The FP32 LU takes its width from RL_TUNE_LU_OUTER_NB.
 template <class T>
 constexpr int outer_nb() {
     return std::is_same<T, float>::value ? 256 : 0;
@@ -212,7 +212,11 @@ rl_status lu_factor_dev(T *A, long long lda, int n, int *ipiv, cudaStream_t s, T
     unsigned long long wns = wait_ns();
     int NBO = n;  // FP32: outer blocks of RL_TUNE_LU_OUTER_NB columns (a multiple of NB)
     if constexpr (std::is_same<T, float>::value) {
-        const int w = (int)(tune(RL_TUNE_LU_OUTER_NB) / NB) * NB;
+        // automatic: at n = 2048 / 4096 one level measured 9.4 / 20.5 ms against 10.5 / 24.2
+        // with 256-column blocks; at 8192 / 16384 512-column blocks 59.1 / 179 ms against
+        // 62.0 / 229 with one level (mixed solves, nrhs 1)
+        const long long v = tune(RL_TUNE_LU_OUTER_NB);
+        const int w = v < 0 ? (n < 6144 ? 0 : 512) : (int)(v / NB) * NB;
         if (w >= NB) NBO = w;
     }
     for (int K0 = 0; K0 < n; K0 += NBO) {

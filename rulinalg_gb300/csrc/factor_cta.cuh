@@ -261,6 +261,34 @@ __device__ __forceinline__ T warp_sum(T v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
+// Warp reduce-scatter of R partial sums per lane (R a power of two <= 32): returns, on
+// every lane, the full sum over the warp of s[row] for row = lane >> (5 - log2 R). The
+// first log2 R butterfly levels halve the values each lane holds (a lane keeps the half
+// of the rows its partner gives away), the rest are a plain butterfly: R - 1 + 5 - log2 R
+// additions per R rows instead of 5 R for a warp_sum per row. A fixed tree: the same
+// inputs always give the same bits.
+template <int R, class T>
+__device__ __forceinline__ T warp_reduce_scatter(T (&s)[R], int lane, int &row) {
+    constexpr int LOG = R >= 32 ? 5 : R >= 16 ? 4 : R >= 8 ? 3 : R >= 4 ? 2 : R >= 2 ? 1 : 0;
+    static_assert((1 << LOG) == R, "R must be a power of two <= 32");
+#pragma unroll
+    for (int lv = 0; lv < LOG; lv++) {
+        const int off = 16 >> lv, half = R >> (lv + 1);
+        const bool up = (lane & off) != 0;
+#pragma unroll
+        for (int k = 0; k < half; k++) {
+            const T keep = up ? s[k + half] : s[k];
+            const T give = up ? s[k] : s[k + half];
+            s[k] = keep + __shfl_xor_sync(0xffffffffu, give, off);
+        }
+    }
+    T v = s[0];
+#pragma unroll
+    for (int off = 16 >> LOG; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    row = lane >> (5 - LOG);
+    return v;
+}
+
 template <class T>
 __device__ __forceinline__ T warp_max(T v) {
 #pragma unroll
@@ -970,7 +998,7 @@ __device__ double copy_rows(const TI *__restrict__ A, int lda, int n, TF *__rest
 #pragma unroll
             for (int c = 0; c < C; c++) {
                 const int i = i0 + r, j = lane + 32 * c;
-                v[r][c] = (i < n && j < n) ? A[(long long)i * lda + j] : TI(0);
+                v[r][c] = (32 * c < n && i < n && j < n) ? A[(long long)i * lda + j] : TI(0);
             }
 #pragma unroll
         for (int r = 0; r < R; r++) {
@@ -978,6 +1006,7 @@ __device__ double copy_rows(const TI *__restrict__ A, int lda, int n, TF *__rest
             TF s = TF(0);
 #pragma unroll
             for (int c = 0; c < C; c++) {
+                if (32 * c >= n) continue;  // warp-uniform: chunks past n do nothing
                 const int j = lane + 32 * c;
                 const TF f = convert_to<TF>(v[r][c]);
                 if (i < n && j < n) W[(long long)i * ldw + j] = f;
@@ -1013,29 +1042,37 @@ __device__ double residual_rows(const TI *__restrict__ A, int lda, const TI *__r
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     double mx = 0.0;
     for (int i0 = warp * R; i0 < n; i0 += CTA_WARPS * R) {
+        // column chunks at or past n are skipped by a warp-uniform test, not zero-filled:
+        // C is fixed per size class (16 chunks for any n in (256, 512])
         TI v[R][C];
 #pragma unroll
         for (int r = 0; r < R; r++)
 #pragma unroll
             for (int c = 0; c < C; c++) {
                 const int i = i0 + r, j = lane + 32 * c;
-                v[r][c] = (i < n && j < n) ? A[(long long)i * lda + j] : TI(0);
+                v[r][c] = (32 * c < n && i < n && j < n) ? A[(long long)i * lda + j] : TI(0);
             }
-        const double bl = (lane < R && i0 + lane < n) ? (double)b[i0 + lane] : 0.0;
+        constexpr int LOG = R >= 4 ? 2 : R >= 2 ? 1 : 0;
+        const int mine = i0 + (lane >> (5 - LOG));  // the row whose sum this lane ends with
+        const double bl = mine < n ? (double)b[mine] : 0.0;
+        double s[R];
 #pragma unroll
         for (int r = 0; r < R; r++) {
-            double s = 0.0;
+            s[r] = 0.0;
 #pragma unroll
             for (int c = 0; c < C; c++) {
                 const int j = lane + 32 * c;
-                s = fma((double)v[r][c], j < n ? S.x()[j] : 0.0, s);
+                if (32 * c < n) s[r] = fma((double)v[r][c], j < n ? S.x()[j] : 0.0, s[r]);
             }
-            s = warp_sum(s);
-            const double ri = __shfl_sync(0xffffffffu, bl, r) - s;
-            if (i0 + r < n) {
-                if (lane == 0) S.r()[i0 + r] = ri;
-                mx = fmax(mx, fabs(ri));
-            }
+        }
+        // the rows' warp sums with R - 1 + 5 - log2 R FP64 additions (a warp-wide FP64
+        // instruction is tens of cycles of the SM's FP64 pipe on this part)
+        int row;
+        const double tot = warp_reduce_scatter<R>(s, lane, row);
+        const double ri = bl - tot;
+        if (i0 + row < n) {
+            if ((lane & ((32 >> LOG) - 1)) == 0) S.r()[i0 + row] = ri;
+            mx = fmax(mx, fabs(ri));
         }
     }
     return mx;
