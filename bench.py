@@ -66,6 +66,7 @@ def parse():
                         "needed to build it; kappa is then ignored)")
     p.add_argument("--lambdas", default="1000,10000,50000", help="serve: arrival rates (requests/s)")
     p.add_argument("--serve-seconds", type=float, default=60.0, help="serve: stream length per rate")
+    p.add_argument("--serve-workers", type=int, default=0, help="serve: worker threads (0: the library's default)")
     p.add_argument("--tune", default="", help="library tunables set before the run: key=value[,key=value] with "
                                               "the RL_TUNE_* keys of include/rulinalg_gb300.h")
     return p.parse_args()
@@ -507,7 +508,7 @@ def config5(dev, args):
             pool[kind].append((np.ascontiguousarray(a), rng.standard_normal(a.shape[0]),
                                [np.zeros(nn) for _ in range(4)]))
     max_pending = 2048
-    srv = rl.Server(max_pending=max_pending)
+    srv = rl.Server(max_pending=max_pending, workers=args.serve_workers)
     resident = []
     for nn in wl.log_uniform_sizes(8, 16, 4096, rng):
         nn = int(nn)
@@ -572,7 +573,8 @@ def config5(dev, args):
     srv.close()
     return {"workload": "Poisson stream, sizes log-uniform [16,4096], 50% LU / 30% Cholesky / 20% QR LS (m=2n), "
                         "30% re-solves of resident factors",
-            "pool_per_kind": per_kind, "resident_factors": len(resident), "max_pending": max_pending, "runs": runs}
+            "pool_per_kind": per_kind, "resident_factors": len(resident), "max_pending": max_pending,
+            "workers": args.serve_workers or "default", "runs": runs}
 
 
 def main():

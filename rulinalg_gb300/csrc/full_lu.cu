@@ -41,65 +41,95 @@ __device__ __forceinline__ double sub_rn<double>(double a, double b) { return __
 template <>
 __device__ __forceinline__ float sub_rn<float>(float a, float b) { return __fsub_rn(a, b); }
 
-// (|v|, row-major index) candidates: larger |v| wins, the smaller index on ties; NaN is
-// never a candidate (|NaN| > x is false in the reference's scan).
+// Candidates are (key, row-major index) pairs. The key of v is |v|'s bit pattern, which
+// orders like |v| for non-NaN values, so the comparisons run on the integer units; a
+// NaN is never a candidate (|NaN| > x is false in the reference's scan). The larger key
+// wins, the smaller index on ties.
 template <class T>
-__device__ __forceinline__ void cand_take(T &bv, long long &bi, T v, long long i) {
-    const T a = absT(v);
-    if (a > bv || (a == bv && i < bi)) {
-        bv = a;
+struct AbsKey;
+template <>
+struct AbsKey<double> {
+    static __device__ __forceinline__ unsigned long long of(double v, bool &nan) {
+        const unsigned long long k = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffULL;
+        nan = k > 0x7ff0000000000000ULL;
+        return k;
+    }
+};
+template <>
+struct AbsKey<float> {
+    static __device__ __forceinline__ unsigned long long of(float v, bool &nan) {
+        const unsigned k = __float_as_uint(v) & 0x7fffffffu;
+        nan = k > 0x7f800000u;
+        return k;
+    }
+};
+
+constexpr long long kNone = LLONG_MAX;
+
+template <class T>
+__device__ __forceinline__ void cand_take(unsigned long long &bk, long long &bi, T v, long long i) {
+    bool nan;
+    const unsigned long long k = AbsKey<T>::of(v, nan);
+    if (!nan && (k > bk || (k == bk && i < bi))) {
+        bk = k;
         bi = i;
     }
 }
 
-template <class T>
-__device__ void block_cand(T &bv, long long &bi, T *sv, long long *si) {
+__device__ __forceinline__ void cand_combine(unsigned long long &bk, long long &bi, unsigned long long k2, long long i2) {
+    if (i2 != kNone && (bi == kNone || k2 > bk || (k2 == bk && i2 < bi))) {
+        bk = k2;
+        bi = i2;
+    }
+}
+
+// Block-wide candidate; every thread gets it. Uses sk / si [warps].
+__device__ void block_cand(unsigned long long &bk, long long &bi, unsigned long long *sk, long long *si) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const T v2 = __shfl_xor_sync(0xffffffffu, bv, o);
-        const long long i2 = __shfl_xor_sync(0xffffffffu, bi, o);
-        if (v2 > bv || (v2 == bv && i2 < bi)) {
-            bv = v2;
-            bi = i2;
-        }
-    }
+    for (int o = 16; o > 0; o >>= 1)
+        cand_combine(bk, bi, __shfl_xor_sync(0xffffffffu, bk, o), __shfl_xor_sync(0xffffffffu, bi, o));
     __syncthreads();
     if (lane == 0) {
-        sv[warp] = bv;
+        sk[warp] = bk;
         si[warp] = bi;
     }
     __syncthreads();
-    bv = sv[0];
+    bk = sk[0];
     bi = si[0];
-    for (int w = 1; w < kFpThreads / 32; w++)
-        if (sv[w] > bv || (sv[w] == bv && si[w] < bi)) {
-            bv = sv[w];
-            bi = si[w];
-        }
+    for (int w = 1; w < kFpThreads / 32; w++) cand_combine(bk, bi, sk[w], si[w]);
 }
 
+constexpr int kFpRowsChunk = 256;  // multipliers staged in shared memory per round
+constexpr int kFpUnroll = 8;       // columns per lane with their loads issued together
+
+// One launch, grid-wide barriers between the steps (cooperative launch). Rows of the
+// trailing block go to CTAs round-robin (row k + 1 + g + m G to CTA g); a CTA forms its
+// rows' multipliers thread-per-row (one division per row, not one per lane), then its
+// warps eliminate one row each at a time, the loads of kFpUnroll columns per lane in
+// flight together.
 template <class T>
 __global__ void __launch_bounds__(kFpThreads) full_piv_lu_kernel(T *A, long long lda, int n, T *W0, T *W1,
-                                                                 long long ldw, int *piv_r, int *piv_c, T *cand_v,
-                                                                 long long *cand_i, PanelSync *sync, int *steps,
+                                                                 long long ldw, int *piv_r, int *piv_c,
+                                                                 unsigned long long *cand_k, long long *cand_i,
+                                                                 PanelSync *sync, int *steps,
                                                                  unsigned long long wait_ns) {
-    __shared__ T sv[kFpThreads / 32];
+    __shared__ unsigned long long sk[kFpThreads / 32];
     __shared__ long long si[kFpThreads / 32];
+    __shared__ T s_l[kFpRowsChunk];
     const int G = gridDim.x, g = blockIdx.x;
-    const int lane = threadIdx.x & 31;
-    const int gw = g * (kFpThreads / 32) + (threadIdx.x >> 5), nw = G * (kFpThreads / 32);
-    const long long NONE = LLONG_MAX;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int gw = g * (kFpThreads / 32) + warp, nw = G * (kFpThreads / 32);
     unsigned phase = 0;
     // candidates of the whole matrix for step 0
     {
-        T bv = T(-1);
-        long long bi = NONE;
+        unsigned long long bk = 0;
+        long long bi = kNone;
         for (int i = gw; i < n; i += nw)
-            for (int j = lane; j < n; j += 32) cand_take(bv, bi, W0[(long long)i * ldw + j], (long long)i * n + j);
-        block_cand(bv, bi, sv, si);
+            for (int j = lane; j < n; j += 32) cand_take(bk, bi, W0[(long long)i * ldw + j], (long long)i * n + j);
+        block_cand(bk, bi, sk, si);
         if (threadIdx.x == 0) {
-            cand_v[g] = bv;  // half 0: read by step 0
+            cand_k[g] = bk;  // half 0: read by step 0
             cand_i[g] = bi;
         }
     }
@@ -108,21 +138,16 @@ __global__ void __launch_bounds__(kFpThreads) full_piv_lu_kernel(T *A, long long
     for (; k < n; k++) {
         T *cur = (k & 1) ? W1 : W0, *nxt = (k & 1) ? W0 : W1;
         // the step's pivot, the same in every CTA
-        T bv = T(-1);
-        long long bi = NONE;
+        unsigned long long bk = 0;
+        long long bi = kNone;
         const int half = (k & 1) * G;
-        for (int q = threadIdx.x; q < G; q += kFpThreads) {
-            const T v = ((volatile T *)cand_v)[half + q];
-            const long long i = ((volatile long long *)cand_i)[half + q];
-            if (v > bv || (v == bv && i < bi)) {
-                bv = v;
-                bi = i;
-            }
-        }
-        block_cand(bv, bi, sv, si);
+        for (int q = threadIdx.x; q < G; q += kFpThreads)
+            cand_combine(bk, bi, ((volatile unsigned long long *)cand_k)[half + q],
+                         ((volatile long long *)cand_i)[half + q]);
+        block_cand(bk, bi, sk, si);
         int r = k, c = k;
         const T akk = cur[(long long)k * ldw + k];
-        if (bi != NONE && !isnan(akk)) {
+        if (bi != kNone && !isnan(akk)) {
             r = (int)(bi / n);
             c = (int)(bi - (long long)r * n);
         }
@@ -146,28 +171,56 @@ __global__ void __launch_bounds__(kFpThreads) full_piv_lu_kernel(T *A, long long
                 A[(long long)i * lda + c] = t;
             }
         // the pivot row: final U row k, read through the swaps (row r, columns swapped)
-        const T *prow = cur + (long long)r * ldw;
+        const T *__restrict__ prow = cur + (long long)r * ldw;
         if (gw == 0)
             for (int j = k + lane; j < n; j += 32) A[(long long)k * lda + j] = prow[j == k ? c : (j == c ? k : j)];
-        // rows below: multiplier into A's column k, eliminated row into nxt; candidates
-        bv = T(-1);
-        bi = NONE;
-        for (int i = k + 1 + gw; i < n; i += nw) {
-            const int src = i == r ? k : i;  // row i after the swap of rows k and r
-            const T *row = cur + (long long)src * ldw;
-            const T l = row[c] / pv;
-            if (lane == 0) A[(long long)i * lda + k] = l;
-            T *out = nxt + (long long)i * ldw;
-            for (int j = k + 1 + lane; j < n; j += 32) {
-                const int sj = j == c ? k : j;  // column j after the swap of columns k and c
-                const T v = sub_rn(row[sj], mul_rn(l, prow[sj]));
-                out[j] = v;
-                cand_take(bv, bi, v, (long long)i * n + j);
+        // this CTA's rows below the pivot: multiplier into A's column k, eliminated row
+        // into nxt, candidates for the next step
+        bk = 0;
+        bi = kNone;
+        const int first = k + 1 + g;
+        const int cnt = first < n ? (n - first + G - 1) / G : 0;
+        for (int m0 = 0; m0 < cnt; m0 += kFpRowsChunk) {
+            const int mc = min(kFpRowsChunk, cnt - m0);
+            for (int t = threadIdx.x; t < mc; t += kFpThreads) {
+                const int i = first + (m0 + t) * G;
+                const int src = i == r ? k : i;  // row i after the swap of rows k and r
+                const T l = cur[(long long)src * ldw + c] / pv;
+                s_l[t] = l;
+                A[(long long)i * lda + k] = l;
             }
+            __syncthreads();
+            for (int t = warp; t < mc; t += kFpThreads / 32) {
+                const int i = first + (m0 + t) * G;
+                const int src = i == r ? k : i;
+                const T *__restrict__ row = cur + (long long)src * ldw;
+                T *__restrict__ out = nxt + (long long)i * ldw;
+                const T l = s_l[t];
+                for (int j0 = k + 1; j0 < n; j0 += 32 * kFpUnroll) {
+                    T a[kFpUnroll], u[kFpUnroll];
+#pragma unroll
+                    for (int q = 0; q < kFpUnroll; q++) {
+                        const int j = j0 + lane + 32 * q;
+                        const int sj = j == c ? k : j;  // column j after the swap of columns k and c
+                        a[q] = j < n ? row[sj] : T(0);
+                        u[q] = j < n ? prow[sj] : T(0);
+                    }
+#pragma unroll
+                    for (int q = 0; q < kFpUnroll; q++) {
+                        const int j = j0 + lane + 32 * q;
+                        if (j < n) {
+                            const T v = sub_rn(a[q], mul_rn(l, u[q]));
+                            out[j] = v;
+                            cand_take(bk, bi, v, (long long)i * n + j);
+                        }
+                    }
+                }
+            }
+            __syncthreads();  // s_l is refilled by the next round
         }
-        block_cand(bv, bi, sv, si);
+        block_cand(bk, bi, sk, si);
         if (threadIdx.x == 0) {
-            cand_v[G - half + g] = bv;  // the other half: read by step k + 1
+            cand_k[G - half + g] = bk;  // the other half: read by step k + 1
             cand_i[G - half + g] = bi;
         }
         if (!grid_barrier(&sync->ctr, (unsigned)(G * (++phase)), &sync->err, wait_ns)) return;
@@ -193,8 +246,12 @@ rl_status full_lu_dev(T *A, long long lda, int n, int *piv_r, int *piv_c, int &s
     int per_sm = 0;
     RL_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFpThreads, 0));
     const long long want = ((long long)n * n + 8LL * kFpThreads - 1) / (8LL * kFpThreads);
-    const int G = (int)std::max<long long>(1, std::min<long long>(want, (long long)std::max(1, per_sm) * num_sms()));
-    DevBuf<T> W0, W1, cv;
+    // at most 3 CTAs per SM: each step ends in a grid barrier and reads every CTA's
+    // candidate, and the elimination is bound by the FP64 pipe, not by loads in flight
+    const int G = (int)std::max<long long>(
+        1, std::min<long long>(want, (long long)std::max(1, std::min(per_sm, 3)) * num_sms()));
+    DevBuf<T> W0, W1;
+    DevBuf<unsigned long long> cv;
     DevBuf<long long> ci;
     DevBuf<PanelSync> sync;
     DevBuf<int> dsteps;
