@@ -84,7 +84,11 @@ RL_API uint64_t rl_launch_count(void);
                                          trailing update is one K = width GEMM on the tensor cores: [-1, 4096],
                                          rounded down to a multiple of 64; 0..63: one level, every 64-column
                                          panel updates the whole trailing matrix; -1 (default): one level for
-                                         n < 6144, 512-column blocks from there (measured best on GB300) */
+                                         n < 6144, 1024-column blocks from there (measured best on GB300) */
+#define RL_TUNE_MIXED_SWEEP_INV 8     /* single-system mixed solves, few right-hand sides: the refinement's
+                                         FP32 triangular sweeps apply each 64 x 64 diagonal block as its
+                                         precomputed inverse (a product) instead of a 64-step substitution:
+                                         [0, 1], default 0 */
 #define RL_TUNE_TEST_WITHHOLD_CHUNK 100 /* tests only: the host batched path never sets this chunk's arrival
                                            flag, so its wait runs out (RL_ERR_TIMEOUT): [-1, 255], default -1 */
 #define RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK 101 /* tests only: the few-right-hand-side triangular sweep never

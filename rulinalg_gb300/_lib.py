@@ -160,6 +160,7 @@ TUNE_BATCH_WARP_COST = 4
 TUNE_UPLOAD_CHUNKS = 5
 TUNE_MIXED_REFINE_STEPS = 6
 TUNE_LU_OUTER_NB = 7
+TUNE_MIXED_SWEEP_INV = 8
 TUNE_TEST_WITHHOLD_CHUNK = 100
 TUNE_TEST_WITHHOLD_SWEEP_BLOCK = 101
 

@@ -213,10 +213,11 @@ rl_status lu_factor_dev(T *A, long long lda, int n, int *ipiv, cudaStream_t s, T
     int NBO = n;  // FP32: outer blocks of RL_TUNE_LU_OUTER_NB columns (a multiple of NB)
     if constexpr (std::is_same<T, float>::value) {
         // automatic: at n = 2048 / 4096 one level measured 9.4 / 20.5 ms against 10.5 / 24.2
-        // with 256-column blocks; at 8192 / 16384 512-column blocks 59.1 / 179 ms against
-        // 62.0 / 229 with one level (mixed solves, nrhs 1)
+        // with 256-column blocks; at 8192 / 16384 1024-column blocks 58.2 / 171 ms against
+        // 59.1 / 179 with 512, 62.4 / 206 with 256 and 62.0 / 229 with one level (mixed
+        // solves, nrhs 1)
         const long long v = tune(RL_TUNE_LU_OUTER_NB);
-        const int w = v < 0 ? (n < 6144 ? 0 : 512) : (int)(v / NB) * NB;
+        const int w = v < 0 ? (n < 6144 ? 0 : 1024) : (int)(v / NB) * NB;
         if (w >= NB) NBO = w;
     }
     for (int K0 = 0; K0 < n; K0 += NBO) {

@@ -51,18 +51,29 @@ inline rl_status colnorm_dev(const double *V, long long ldv, int n, int nrhs, un
     return RL_OK;
 }
 
+// Inverted 64 x 64 diagonal blocks of the two triangles of an FP32 factor (FP32, formed
+// once) and the sweep flags that use them: the form of RL_TUNE_MIXED_SWEEP_INV.
+struct SweepInv {
+    const float *D1 = nullptr, *D2 = nullptr;
+    int *ctl = nullptr;  // 2 x (1 + blocks) words, zeroed before each pair of sweeps
+};
+
 // W <- M^-1 W with the FP32 factor (LU: ipiv swaps, unit L, U; Cholesky: L, L^T). No
-// absolute-epsilon rule here: only a pivot below FLT_MIN counts as singular.
+// absolute-epsilon rule here: only a pivot below FLT_MIN counts as singular. With inv.D1
+// set, the sweeps apply the diagonal blocks' inverses (few right-hand sides only).
 inline rl_status precond_solve(const float *F, int n, int kind, const int *ipiv, float *W, long long ldw, int nrhs,
-                        int *dstatus, cudaStream_t s) {
+                               int *dstatus, cudaStream_t s, const SweepInv &inv = SweepInv()) {
     const float tiny = FLT_MIN;
-    if (kind == RL_KIND_LU) {
-        RL_TRY(laswp<float>(W, ldw, nrhs, 0, 0, ipiv, 0, n, s));
-        RL_TRY(tri_solve_dev<float>(F, n, n, W, ldw, nrhs, 0, dstatus, s, tiny));
-        return tri_solve_dev<float>(F, n, n, W, ldw, nrhs, 2, dstatus, s, tiny);
+    const int m1 = kind == RL_KIND_LU ? 0 : 1, m2 = kind == RL_KIND_LU ? 2 : 3;
+    if (kind == RL_KIND_LU) RL_TRY(laswp<float>(W, ldw, nrhs, 0, 0, ipiv, 0, n, s));
+    if (inv.D1 && nrhs <= kSweepRhs) {
+        const int words = 1 + ceil_div(n, kSweepRows);
+        RL_TRY_CUDA(cudaMemsetAsync(inv.ctl, 0, 2 * words * sizeof(int), s));
+        RL_TRY((tri_solve_inv_dev<float, float>(F, n, n, inv.D1, W, ldw, nrhs, m1, dstatus, s, tiny, inv.ctl)));
+        return tri_solve_inv_dev<float, float>(F, n, n, inv.D2, W, ldw, nrhs, m2, dstatus, s, tiny, inv.ctl + words);
     }
-    RL_TRY(tri_solve_dev<float>(F, n, n, W, ldw, nrhs, 1, dstatus, s, tiny));
-    return tri_solve_dev<float>(F, n, n, W, ldw, nrhs, 3, dstatus, s, tiny);
+    RL_TRY(tri_solve_dev<float>(F, n, n, W, ldw, nrhs, m1, dstatus, s, tiny));
+    return tri_solve_dev<float>(F, n, n, W, ldw, nrhs, m2, dstatus, s, tiny);
 }
 
 // dst = M^-1 src for one FP64 vector with the solves in FP32 (the vector scaled by its
@@ -297,6 +308,7 @@ struct MixedFactor {
     bool f32_ok = false;
     double *F64 = nullptr;
     int *ipiv64 = nullptr;
+    float *Dinv = nullptr;  // RL_TUNE_MIXED_SWEEP_INV: both triangles' inverted diagonal blocks
     rl_status f64_status = RL_OK;
     bool f64_ready = false;
     cudaStream_t home = nullptr;  // stream the buffers were allocated on
@@ -307,17 +319,29 @@ struct MixedFactor {
     ~MixedFactor() { release(); }
 
     void release() {
-        void *ps[] = {A_own, F, ipiv, F64, ipiv64};
+        void *ps[] = {A_own, F, ipiv, F64, ipiv64, Dinv};
         for (void *p : ps)
             if (p) cudaFreeAsync(p, home);
-        A_own = nullptr, F = nullptr, ipiv = nullptr, F64 = nullptr, ipiv64 = nullptr;
+        A_own = nullptr, F = nullptr, ipiv = nullptr, F64 = nullptr, ipiv64 = nullptr, Dinv = nullptr;
     }
+
+    size_t dinv_elems() const { return (size_t)ceil_div(n, kSweepRows) * kSweepRows * kSweepRows; }
 
     size_t bytes() const {
         size_t b = (size_t)n * n * sizeof(float) + (size_t)n * sizeof(int);
         if (A_own) b += (size_t)n * n * sizeof(double);
         if (F64) b += (size_t)n * n * sizeof(double) + (size_t)n * sizeof(int);
+        if (Dinv) b += 2 * dinv_elems() * sizeof(float);
         return b;
+    }
+
+    // The inverted diagonal blocks for the sweeps (formed on first use).
+    rl_status ensure_dinv(int *dstatus, cudaStream_t s) {
+        if (Dinv) return RL_OK;
+        RL_TRY(alloc(Dinv, 2 * dinv_elems(), s));
+        const int m1 = kind == RL_KIND_LU ? 0 : 1, m2 = kind == RL_KIND_LU ? 2 : 3;
+        RL_TRY((diag_inverse<float, float>(F, n, n, m1, Dinv, dstatus, s, FLT_MIN)));
+        return diag_inverse<float, float>(F, n, n, m2, Dinv + dinv_elems(), dstatus, s, FLT_MIN);
     }
 
     template <class T>
@@ -414,6 +438,13 @@ struct MixedFactor {
         RL_TRY(nb.alloc(3 * nrhs, s));
         unsigned long long *bn_b = nb.p, *rn_b = nb.p + nrhs, *xn_b = nb.p + 2 * nrhs;
         RL_TRY_CUDA(cudaMemsetAsync(dstatus.p, 0, 2 * sizeof(int), s));
+        SweepInv inv;
+        DevBuf<int> sweep_ctl;
+        if (tune(RL_TUNE_MIXED_SWEEP_INV) && nrhs <= kSweepRhs && n > CTA_NMAX) {
+            RL_TRY(ensure_dinv(dstatus.p, s));
+            RL_TRY(sweep_ctl.alloc(2 * (size_t)(1 + ceil_div(n, kSweepRows)), s));
+            inv = SweepInv{Dinv, Dinv + dinv_elems(), sweep_ctl.p};
+        }
         std::vector<int> act(nrhs + 1, 1);
         RL_TRY_CUDA(cudaMemcpyAsync(active.p, act.data(), act.size() * sizeof(int), cudaMemcpyHostToDevice, s));
         RL_TRY(colnorm_dev(B, ldb, n, nrhs, bn_b, s));
@@ -423,7 +454,7 @@ struct MixedFactor {
         std::vector<double> prev(nrhs, INFINITY), bnorm(nrhs, 0.0);
         // x0 = M^-1 b
         RL_LAUNCH(scale_to_f32_kernel, ge, 256, 0, s, B, ldb, n, nrhs, bn_b, W.p, (long long)nrhs);
-        RL_TRY(precond_solve(F, n, kind, ipiv, W.p, nrhs, nrhs, dstatus.p, s));
+        RL_TRY(precond_solve(F, n, kind, ipiv, W.p, nrhs, nrhs, dstatus.p, s, inv));
         RL_TRY_CUDA(cudaMemset2DAsync(X, ldx * sizeof(double), 0, nrhs * sizeof(double), n, s));
         RL_LAUNCH(update_x_kernel, ge, 256, 0, s, X, ldx, W.p, (long long)nrhs, n, nrhs, bn_b, active.p);
         std::vector<unsigned long long> hb(3 * nrhs);
@@ -473,7 +504,7 @@ struct MixedFactor {
             }
             RL_TRY_CUDA(cudaMemcpyAsync(active.p, act.data(), nrhs * sizeof(int), cudaMemcpyHostToDevice, s));
             RL_LAUNCH(scale_to_f32_kernel, ge, 256, 0, s, R.p, (long long)nrhs, n, nrhs, rn_b, W.p, (long long)nrhs);
-            RL_TRY(precond_solve(F, n, kind, ipiv, W.p, nrhs, nrhs, dstatus.p, s));
+            RL_TRY(precond_solve(F, n, kind, ipiv, W.p, nrhs, nrhs, dstatus.p, s, inv));
             RL_LAUNCH(update_x_kernel, ge, 256, 0, s, X, ldx, W.p, (long long)nrhs, n, nrhs, rn_b, active.p);
         }
         if (!need_fp64) {

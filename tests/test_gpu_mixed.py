@@ -135,3 +135,42 @@ def test_gmres_ir_taken_and_converges(gpu):
     fe = np.linalg.norm(x - xo) / np.linalg.norm(xo)
     assert fe <= 2 * kappa * (eta(x) + eta(xo)), (fe, info)
     print(f"GMRES-IR n={n} kappa={kappa:.0e}: {info}, forward error vs oracle {fe:.2e}")
+
+
+@pytest.mark.parametrize("kind", ["lu", "cholesky"])
+@pytest.mark.parametrize("kappa", [1e2, 1e6])
+def test_mixed_sweeps_with_inverted_diagonal_blocks(gpu, kind, kappa):
+    """RL_TUNE_MIXED_SWEEP_INV = 1: the refinement's triangular sweeps apply each 64 x 64
+    diagonal block as its FP32 inverse. The solution is as accurate as with substitution
+    (f64 backward error, forward error within the oracle bound); at kappa = 1e2 it takes
+    the same path in at most two more refinement steps."""
+    from rulinalg_gb300 import _lib as L
+    from rulinalg_gb300.workloads import conditioned_system
+    n = 1500
+    a, b = conditioned_system(n, kappa, 2, seed=77 + int(np.log10(kappa)))
+    if kind == "cholesky":
+        a = a @ a.T  # SPD with kappa^2
+    saved = gpu.tune_get(L.TUNE_MIXED_SWEEP_INV)
+    try:
+        gpu.tune_set(L.TUNE_MIXED_SWEEP_INV, 0)
+        x0, i0 = gpu.solve_mixed(a, b, kind)
+        gpu.tune_set(L.TUNE_MIXED_SWEEP_INV, 1)
+        x1, i1 = gpu.solve_mixed(a, b, kind)
+    finally:
+        gpu.tune_set(L.TUNE_MIXED_SWEEP_INV, saved)
+    if kind == "lu":
+        f, perm, st = O.lu_decompose(a, threads=8)
+    else:
+        f, st = O.chol_decompose(a)
+        perm = None
+    assert st == O.OK
+    xo, _ = O.solve_columns(f, perm, b, threads=8)
+    k = kappa if kind == "lu" else kappa ** 2
+    eta = lambda v, c: np.linalg.norm(b[:, c] - a @ v) / (np.linalg.norm(a, 2) * np.linalg.norm(v) + np.linalg.norm(b[:, c]))
+    for c in range(2):
+        assert backward_error(a, x1[:, c], b[:, c]) <= n * U64 * 10, (c, i1)
+        fe = np.linalg.norm(x1[:, c] - xo[:, c]) / np.linalg.norm(xo[:, c])
+        assert fe <= 2 * k * (eta(x1[:, c], c) + eta(xo[:, c], c)), (c, fe, i1)
+    if kappa == 1e2:
+        assert i0["path"] == i1["path"] == "refinement" and i1["iters"] <= i0["iters"] + 2, (i0, i1)
+    print(f"{kind} kappa={kappa:.0e}: substitution {i0}, inverted blocks {i1}")
