@@ -846,201 +846,91 @@ __device__ __noinline__ int diag_block_solve(const T *__restrict__ A, int lda, i
     return bad;
 }
 
-// One triangular solve on S.w, 32-row blocks in solve order, with the memory traffic
-// of a block off its critical path. While warp 0 solves the diagonal block (from
-// registers it loaded during the previous block's update), warps 1..7 load their first
-// pass of the block's off-diagonal rows; after the barrier they apply them, and warp 0
-// loads the next diagonal block, whose registers are first read after the next barrier.
-// Without this each block waited for two dependent round trips to L2 or DRAM (the
-// diagonal block, then the off-diagonal rows) besides its 32-step solve.
-//   FORWARD: top-down (L y = w), else bottom-up (U x = w or L^T x = w);
-//   UNIT: unit diagonal (not read); TRANS: the transpose of the lower triangle (L^T).
-// A diagonal entry below tiny returns RL_ERR_DIV_BY_ZERO (src/matrix/mod.rs:333-336,
-// 375-378). The arithmetic is diag_block_solve's and cta_block_update's (the same sums in
-// the same order): only the timing of the loads changed.
-// Rows r < bs of a 32 x 32 diagonal block at (b0, b0), column lane, into registers.
-template <class T>
-__device__ __forceinline__ void load_diag_block(const T *__restrict__ A, int lda, int b0, int bs, int lane,
-                                                T (&v)[32]) {
-#pragma unroll
-    for (int r = 0; r < 32; r++) v[r] = (r < bs && lane < bs) ? A[(long long)(b0 + r) * lda + b0 + lane] : T(0);
-}
-
-// Barrier 1 of the CTA, reached from the two roles' separate code paths of
-// cta_tri_solve (bar.sync counts arrivals; every thread of the CTA arrives).
-__device__ __forceinline__ void role_barrier() { asm volatile("bar.sync 1, %0;" ::"n"(CTA_THREADS) : "memory"); }
-
-template <class T, bool FORWARD, bool UNIT, bool TRANS>
-__device__ __noinline__ int cta_tri_solve(const T *__restrict__ A, int lda, int n, CtaSmem<T> &S, T tiny) {
-    constexpr int RB = sizeof(T) == 4 ? 32 : 16;     // rows per warp pass (non-transposed)
-    constexpr bool PREFETCH_DIAG = sizeof(T) == 4;  // 32 more registers: FP32 only
-    constexpr int UW = CTA_WARPS - 1;               // update warps
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int nb = (n + 31) / 32;
-    auto block = [n](int kb, int &b0, int &bs) {
-        if (FORWARD) {
-            b0 = kb * 32;
-            bs = min(32, n - b0);
-        } else {
-            const int b1 = n - kb * 32;
-            b0 = max(0, b1 - 32);
-            bs = b1 - b0;
-        }
-    };
-    // Each block: [phase A] barrier [status check] [phase B] barrier. The two roles run
-    // separate loops (so that neither keeps the other's registers live) and meet at
-    // the same barriers in the same order.
-    if (warp == 0) {
-        T dv[32];
-        if (PREFETCH_DIAG) {
-            int b0, bs;
-            block(0, b0, bs);
-            load_diag_block(A, lda, b0, bs, lane, dv);
-        }
-        for (int kb = 0; kb < nb; kb++) {
-            int b0, bs;
-            block(kb, b0, bs);
-            // phase A: the diagonal block's solve
-            T *D = S.P;
-            if (!PREFETCH_DIAG) load_diag_block(A, lda, b0, bs, lane, dv);
-#pragma unroll
-            for (int r = 0; r < 32; r++) D[r * 33 + lane] = dv[r];
-            __syncwarp();
-            auto elem = [D, lane](int c) { return TRANS ? D[c * 33 + lane] : D[lane * 33 + c]; };
-            const T d = UNIT ? T(1) : elem(lane);
-            const int bad = UNIT ? 0 : __any_sync(0xffffffffu, lane < bs && absT(d) < tiny);
-            const T inv = T(1) / d;
-            T wv = lane < bs ? S.w[b0 + lane] : T(0);
-            if (FORWARD) {
-#pragma unroll 4
-                for (int jj = 0; jj < bs; jj++) {
-                    if (!UNIT && lane == jj) wv = solve_div(wv, d, inv);
-                    const T wj = __shfl_sync(0xffffffffu, wv, jj);
-                    if (lane > jj) wv = fma(-elem(jj), wj, wv);
-                }
-            } else {
-#pragma unroll 4
-                for (int jj = bs - 1; jj >= 0; jj--) {
-                    if (!UNIT && lane == jj) wv = solve_div(wv, d, inv);
-                    const T wj = __shfl_sync(0xffffffffu, wv, jj);
-                    if (lane < jj) wv = fma(-elem(jj), wj, wv);
-                }
-            }
-            if (lane < bs) S.w[b0 + lane] = wv;
-            if (lane == 0) S.status = bad;
-            role_barrier();
-            if (!UNIT && S.status) {
-                role_barrier();
-                return RL_ERR_DIV_BY_ZERO;
-            }
-            // phase B: the next diagonal block's loads (first read after the next barrier)
-            if (PREFETCH_DIAG && kb + 1 < nb) {
-                int nb0, nbs;
-                block(kb + 1, nb0, nbs);
-                load_diag_block(A, lda, nb0, nbs, lane, dv);
-            }
-            role_barrier();
-        }
-        return RL_OK;
-    }
-    for (int kb = 0; kb < nb; kb++) {
-        int b0, bs;
-        block(kb, b0, bs);
-        const int lo = FORWARD ? b0 + bs : 0, hi = FORWARD ? n : b0;
-        if (!TRANS) {
-            // phase A: the first pass of this warp's off-diagonal rows into registers
-            T p[RB];
-            const int rw = lo + (warp - 1) * RB;
-#pragma unroll
-            for (int r = 0; r < RB; r++) {
-                const int i = rw + r;
-                p[r] = (i < hi && lane < bs) ? A[(long long)i * lda + b0 + lane] : T(0);
-            }
-            role_barrier();
-            if (!UNIT && S.status) {
-                role_barrier();
-                return RL_ERR_DIV_BY_ZERO;
-            }
-            // phase B: w[i] -= sum_c M[i][c] w[b0 + c], a butterfly reduce-scatter leaving
-            // row r's sum in lane r
-            const T y = lane < bs ? S.w[b0 + lane] : T(0);
-            for (int r0 = rw, pass = 0; r0 < hi; r0 += UW * RB, pass++) {
-                if (pass > 0)
-#pragma unroll
-                    for (int r = 0; r < RB; r++) {
-                        const int i = r0 + r;
-                        p[r] = (i < hi && lane < bs) ? A[(long long)i * lda + b0 + lane] : T(0);
-                    }
-#pragma unroll
-                for (int r = 0; r < RB; r++) p[r] *= y;
-#pragma unroll
-                for (int sh = 16; sh >= RB; sh >>= 1)
-#pragma unroll
-                    for (int r = 0; r < RB; r++) p[r] += __shfl_xor_sync(0xffffffffu, p[r], sh);
-#pragma unroll
-                for (int sh = RB / 2; sh >= 1; sh >>= 1) {
-                    const bool up = lane & sh;
-#pragma unroll
-                    for (int k = 0; k < sh; k++) {
-                        const T send = up ? p[k] : p[k + sh];
-                        const T keep = up ? p[k + sh] : p[k];
-                        p[k] = keep + __shfl_xor_sync(0xffffffffu, send, sh);
-                    }
-                }
-                const int i = r0 + (lane & (RB - 1));
-                if (lane < RB && i < hi) S.w[i] -= p[0];
-            }
-        } else {
-            // L^T: w[i] -= sum_jj L[b0 + jj][i] w[b0 + jj] for i < b0, a thread per i
-            // (coalesced rows); phase A loads the first pass
-            T tv[32];
-            const int iw = lo + tid - 32;
-#pragma unroll
-            for (int jj = 0; jj < 32; jj++) tv[jj] = (iw < hi && jj < bs) ? A[(long long)(b0 + jj) * lda + iw] : T(0);
-            role_barrier();
-            if (!UNIT && S.status) {
-                role_barrier();
-                return RL_ERR_DIV_BY_ZERO;
-            }
-            for (int i = iw, pass = 0; i < hi; i += UW * 32, pass++) {
-                if (pass > 0)
-#pragma unroll
-                    for (int jj = 0; jj < 32; jj++) tv[jj] = jj < bs ? A[(long long)(b0 + jj) * lda + i] : T(0);
-                T sum = T(0);
-#pragma unroll
-                for (int jj = 0; jj < 32; jj++)
-                    if (jj < bs) sum = fma(tv[jj], S.w[b0 + jj], sum);
-                S.w[i] -= sum;
-            }
-        }
-        role_barrier();
-    }
-    return RL_OK;
-}
-
 // Unit lower triangular solve L y = w (L strictly below the diagonal of A).
 template <class T>
 __device__ void cta_unit_lower_solve(const T *__restrict__ A, int lda, int n, CtaSmem<T> &S) {
-    cta_tri_solve<T, true, true, false>(A, lda, n, S, T(0));
+    const int warp = threadIdx.x >> 5;
+    for (int b0 = 0; b0 < n; b0 += 32) {
+        const int bs = min(32, n - b0);
+        if (warp == 0) diag_block_solve<T, true, true, false>(A, lda, b0, bs, S, T(0));
+        __syncthreads();
+        cta_block_update(A + b0, lda, b0 + bs, n, b0, bs, S);
+        __syncthreads();
+    }
 }
 
 // Upper triangular solve U x = w (U on and above the diagonal of A). |u_ii| < tiny
 // returns RL_ERR_DIV_BY_ZERO (src/matrix/mod.rs:333-336).
 template <class T>
 __device__ int cta_upper_solve(const T *__restrict__ A, int lda, int n, CtaSmem<T> &S, T tiny) {
-    return cta_tri_solve<T, false, false, false>(A, lda, n, S, tiny);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int b1 = n; b1 > 0; b1 -= 32) {
+        const int b0 = max(0, b1 - 32), bs = b1 - b0;
+        if (warp == 0) {
+            const int bad = diag_block_solve<T, false, false, false>(A, lda, b0, bs, S, tiny);
+            if (lane == 0) S.status = bad;
+        }
+        __syncthreads();
+        if (S.status) {
+            __syncthreads();
+            return RL_ERR_DIV_BY_ZERO;
+        }
+        cta_block_update(A + b0, lda, 0, b0, b0, bs, S);
+        __syncthreads();
+    }
+    return RL_OK;
 }
 
 // Lower (non-unit) solve L y = w; |l_ii| < tiny -> RL_ERR_DIV_BY_ZERO (mod.rs:375-378).
 template <class T>
 __device__ int cta_lower_solve(const T *__restrict__ A, int lda, int n, CtaSmem<T> &S, T tiny) {
-    return cta_tri_solve<T, true, false, false>(A, lda, n, S, tiny);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int b0 = 0; b0 < n; b0 += 32) {
+        const int bs = min(32, n - b0);
+        if (warp == 0) {
+            const int bad = diag_block_solve<T, true, false, false>(A, lda, b0, bs, S, tiny);
+            if (lane == 0) S.status = bad;
+        }
+        __syncthreads();
+        if (S.status) {
+            __syncthreads();
+            return RL_ERR_DIV_BY_ZERO;
+        }
+        cta_block_update(A + b0, lda, b0 + bs, n, b0, bs, S);
+        __syncthreads();
+    }
+    return RL_OK;
 }
 
 // Transposed solve L^T x = w with L lower (cholesky.rs:329-361).
 template <class T>
 __device__ int cta_lower_t_solve(const T *__restrict__ A, int lda, int n, CtaSmem<T> &S, T tiny) {
-    return cta_tri_solve<T, false, false, true>(A, lda, n, S, tiny);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int b1 = n; b1 > 0; b1 -= 32) {
+        const int b0 = max(0, b1 - 32), bs = b1 - b0;
+        if (warp == 0) {
+            const int bad = diag_block_solve<T, false, false, true>(A, lda, b0, bs, S, tiny);
+            if (lane == 0) S.status = bad;
+        }
+        __syncthreads();
+        if (S.status) {
+            __syncthreads();
+            return RL_ERR_DIV_BY_ZERO;
+        }
+        // w[i] -= sum_jj L[b0 + jj][i] w[b0 + jj] for i < b0: a thread per i, coalesced rows
+        for (int i = tid; i < b0; i += CTA_THREADS) {
+            T v[32];
+#pragma unroll
+            for (int jj = 0; jj < 32; jj++) v[jj] = jj < bs ? A[(long long)(b0 + jj) * lda + i] : T(0);
+            T s = T(0);
+#pragma unroll
+            for (int jj = 0; jj < 32; jj++)
+                if (jj < bs) s = fma(v[jj], S.w[b0 + jj], s);
+            S.w[i] -= s;
+        }
+        __syncthreads();
+    }
+    return RL_OK;
 }
 
 // Row permutation of an LU factorisation as a position -> original row map (from the
