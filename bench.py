@@ -133,6 +133,48 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
+def parse_cpulist(text: str) -> set:
+    cpus = set()
+    for part in text.strip().split(","):
+        if not part:
+            continue
+        if "-" in part:
+            a, b = part.split("-")
+            cpus.update(range(int(a), int(b) + 1))
+        else:
+            cpus.add(int(part))
+    return cpus
+
+
+def pin_near_gpu(index: int) -> str:
+    """Restricts this process to the host CPUs local to GPU `index` (sysfs local_cpulist of
+    its PCI function), so that the pinned host buffers the end-to-end leg allocates and
+    first touches sit in the memory attached to that GPU's host link. Returns what was
+    done, for the JSON line."""
+    try:
+        import torch
+        p = torch.cuda.get_device_properties(index)
+        bdf = f"{p.pci_domain_id:04x}:{p.pci_bus_id:02x}:{p.pci_device_id:02x}.0"
+    except Exception:
+        try:
+            out = subprocess.run(["nvidia-smi", "-i", str(index), "--query-gpu=pci.bus_id", "--format=csv,noheader"],
+                                 capture_output=True, text=True, timeout=10).stdout.strip()
+            dom, bus, rest = out.split(":")
+            bdf = f"{int(dom, 16):04x}:{bus.lower()}:{rest.lower()}"
+        except Exception as e:  # no affinity information: leave the process as it is
+            return f"unchanged ({type(e).__name__})"
+    try:
+        cpus = parse_cpulist(Path(f"/sys/bus/pci/devices/{bdf}/local_cpulist").read_text())
+        allowed = os.sched_getaffinity(0)
+        use = cpus & allowed
+        if not use or use == allowed:
+            return f"unchanged (local CPUs of {bdf}: {len(cpus)}, allowed {len(allowed)})"
+        os.sched_setaffinity(0, use)
+        return f"{len(use)} CPUs local to GPU {bdf} (of {len(allowed)})"
+    except Exception as e:
+        return f"unchanged ({type(e).__name__})"
+
+
 def flops_of(n, kind):
     n = n.astype(np.float64)
     return float(np.sum(np.where(kind == 1, n ** 3 / 3.0, 2.0 * n ** 3 / 3.0)))
@@ -595,6 +637,7 @@ def main():
     torch.cuda.set_device(dev)
     if not rl.device_available():
         raise SystemExit("rulinalg_gb300: no usable sm_103 GPU")
+    affinity = pin_near_gpu(local)
     for kv in filter(None, args.tune.split(",")):
         k, v = kv.split("=")
         rl.tune_set(int(k), int(float(v)))
@@ -699,7 +742,9 @@ def main():
         e2e_s = aggregate_max(statistics.mean(ts), world, dev)
         e2e = {"value": world * count / e2e_s, "unit": "solves/s", "ms_per_step": 1e3 * e2e_s,
                "h2d_bytes_per_step": int(a_bytes + b_bytes),
-               "d2h_bytes_per_step": int(b_bytes + count * (4 + 4 + 8))}
+               "d2h_bytes_per_step": int(b_bytes + count * (4 + 4 + 8)),
+               "ms_steps": [round(1e3 * t, 2) for t in ts], "host_affinity": affinity,
+               "timing": "host clock around each rl_dbatch_solve call (pinned host buffers in, results out)"}
         assert np.array_equal(x_h.numpy(), mixed["x"].cpu().numpy()), "host and device entry points disagree"
 
     # accuracy of both paths (f64 backward error bound n 2^-53 10)

@@ -76,3 +76,11 @@ def test_bench_profile_traffic_line(tmp_path):
     p.write_text("traffic_per_launch_bytes: 99200000000\n")
     assert bench.profile_traffic(1.0, p) is None
     assert bench.profile_traffic(1.0) is not None  # the committed profile carries the line
+
+
+def test_bench_cpulist_parse():
+    """bench.py's sysfs local_cpulist parser (used to keep the end-to-end leg's pinned
+    buffers on the GPU's own host memory)."""
+    import bench
+    assert bench.parse_cpulist("0-3,8,10-11\n") == {0, 1, 2, 3, 8, 10, 11}
+    assert bench.parse_cpulist("72-143") == set(range(72, 144))
