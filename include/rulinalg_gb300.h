@@ -85,7 +85,7 @@ RL_API uint64_t rl_launch_count(void);
                                          rounded down to a multiple of 64; 0..63: one level, every 64-column
                                          panel updates the whole trailing matrix; -1 (default): one level for
                                          n < 6144, 1024-column blocks from there (measured best on GB300) */
-#define RL_TUNE_MIXED_SWEEP_INV 8     /* single-system mixed solves, few right-hand sides: the refinement's
+#define RL_TUNE_MIXED_SWEEP_INV 8     /* single-system mixed solves, up to 128 right-hand sides: the refinement's
                                          FP32 triangular sweeps apply each 64 x 64 diagonal block as its
                                          precomputed inverse (a product) instead of a 64-step substitution:
                                          [0, 1], default 1 (1-7% faster at n = 4096-16384, same refinement

@@ -798,8 +798,22 @@ static __global__ void __launch_bounds__(128) trsm_diag_kernel(const T *D, long 
 // x_b = Dinv_b (y_b - folded sums), 16-term dot products over all 256 threads, instead
 // of the 64-step substitution chain: in FP64 that chain's dependent DFMAs cost ~20 us
 // per block on this part.
-// Per-launch state: ctl[0] = ticket, ctl[1 + b] = block b published, zeroed by the host.
-constexpr int kSweepRows = 64, kSweepRhs = 8, kSweepCtas = 32;
+// More than kSweepRhs right-hand sides run as groups of kSweepRhs columns side by side:
+// blockIdx.y is the group, with its own ticket and block flags; groups never wait on one
+// another.
+// Per-launch state, per group g: ctl[g (1 + nb)] = ticket, ctl[g (1 + nb) + 1 + b] =
+// block b published, zeroed by the host.
+constexpr int kSweepRows = 64, kSweepRhs = 8, kSweepCtas = 32, kSweepGroups = 16;
+
+// Right-hand-side groups of a sweep over nrhs columns, 0 when the sweep does not take
+// them (more than kSweepGroups groups); ctl words it needs for n rows.
+inline int sweep_groups(int nrhs) {
+    const int g = (nrhs + kSweepRhs - 1) / kSweepRhs;
+    return g <= kSweepGroups ? g : 0;
+}
+inline int sweep_ctl_words(int n, int nrhs) {
+    return sweep_groups(nrhs) * (1 + (n + kSweepRows - 1) / kSweepRows);
+}
 template <class T, class TA = T>
 static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const TA *__restrict__ A, long long lda, int n,
                                                              T *__restrict__ Y, long long ldy, int nrhs, int mode,
@@ -814,6 +828,10 @@ static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const TA *__rest
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nb = (n + BR - 1) / BR;
     const bool fwd = mode <= 1, trans = mode == 3;
+    // this CTA's group of right-hand sides
+    Y += (long long)blockIdx.y * kSweepRhs;
+    nrhs = min(kSweepRhs, nrhs - (int)blockIdx.y * kSweepRhs);
+    ctl += (long long)blockIdx.y * (1 + nb);
     if (tid == 0) s_fail = 0;
     for (;;) {
         __syncthreads();  // the previous block's shared state is no longer read

@@ -459,8 +459,8 @@ rl_status qr_apply_q_dev(const T *QR, long long lda, int m, int n, const T *tau,
 // Blocked triangular solve op(A) X = Y in place (A n x n, Y n x nrhs).
 // mode 0: unit lower, 1: lower, 2: upper, 3: L^T with L lower. |d_ii| < eps is
 // recorded as RL_ERR_DIV_BY_ZERO in *dstatus. A may be stored in a narrower type TA than
-// the arithmetic type T for at most kSweepRhs right-hand sides (an FP32 factor applied in
-// FP64).
+// the arithmetic type T for at most kSweepGroups x kSweepRhs right-hand sides (an FP32
+// factor applied in FP64), kSweepRhs on a GPU shared with other workers.
 template <class T, class TA>
 rl_status tri_solve_dev(const TA *A, long long lda, int n, T *Y, long long ldy, int nrhs, int mode, int *dstatus,
                         cudaStream_t s, T tiny) {
@@ -499,15 +499,18 @@ rl_status tri_solve_dev(const TA *A, long long lda, int n, T *Y, long long ldy, 
         }
         return RL_OK;
     }
-    if (nrhs <= kSweepRhs) {
-        // Few right-hand sides: the whole solve in one launch (trsv_sweep_kernel); a GEMM
-        // tile per block would waste all but nrhs of its columns.
-        const int nb = ceil_div(n, kSweepRows);
+    if (sweep_groups(nrhs) > 0 && !g_shared_gpu) {
+        // Up to kSweepGroups x kSweepRhs right-hand sides: the whole solve in one launch
+        // (trsv_sweep_kernel, groups of kSweepRhs columns side by side). The blocked form
+        // below costs two launches per 64-row block, a 64-step chain on a few CTAs and a
+        // GEMM whose tiles would be mostly empty.
+        const int nb = ceil_div(n, kSweepRows), words = sweep_ctl_words(n, nrhs);
         DevBuf<int> ctl;
-        RL_TRY(ctl.alloc(1 + nb, s));
-        RL_TRY_CUDA(cudaMemsetAsync(ctl.p, 0, sizeof(int) * (1 + nb), s));
-        RL_LAUNCH((trsv_sweep_kernel<T, TA>), std::min(nb, kSweepCtas), 256, 0, s, A, lda, n, Y, ldy, nrhs, mode, ctl.p, dstatus,
-                  tiny, wait_ns(), (int)tune(RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK), (const T *)nullptr);
+        RL_TRY(ctl.alloc(words, s));
+        RL_TRY_CUDA(cudaMemsetAsync(ctl.p, 0, sizeof(int) * words, s));
+        RL_LAUNCH((trsv_sweep_kernel<T, TA>), dim3(std::min(nb, kSweepCtas), sweep_groups(nrhs)), 256, 0, s, A, lda, n, Y,
+                  ldy, nrhs, mode, ctl.p, dstatus, tiny, wait_ns(), (int)tune(RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK),
+                  (const T *)nullptr);
         return RL_OK;
     }
     if constexpr (!std::is_same<T, TA>::value) {
@@ -553,18 +556,21 @@ rl_status diag_inverse(const TA *A, long long lda, int n, int mode, T *Dinv, int
     return RL_OK;
 }
 
-// op(A) Y = Y' for at most kSweepRhs right-hand sides in one sweep launch whose block
-// solves are products with the diagonal blocks' inverses Dinv (diag_inverse). ctl:
-// 1 + ceil(n / 64) zeroed ints (the sweep's ticket and block flags). More right-hand
-// sides, or a GPU shared with other streams of this library (the serving workers, see
-// tri_solve_dev), take tri_solve_dev's substitution paths instead.
+// op(A) Y = Y' for at most kSweepGroups x kSweepRhs right-hand sides in one sweep launch
+// whose block solves are products with the diagonal blocks' inverses Dinv
+// (diag_inverse). ctl: sweep_ctl_words(n, nrhs) zeroed ints (each group's ticket and
+// block flags). More right-hand sides, or a GPU shared with other streams of this
+// library (the serving workers, see tri_solve_dev), take tri_solve_dev's substitution
+// paths instead.
 template <class T, class TA>
 rl_status tri_solve_inv_dev(const TA *A, long long lda, int n, const T *Dinv, T *Y, long long ldy, int nrhs, int mode,
                             int *dstatus, cudaStream_t s, T tiny, int *ctl) {
-    if (nrhs > kSweepRhs || g_shared_gpu) return tri_solve_dev<T, TA>(A, lda, n, Y, ldy, nrhs, mode, dstatus, s, tiny);
+    if (sweep_groups(nrhs) == 0 || g_shared_gpu)
+        return tri_solve_dev<T, TA>(A, lda, n, Y, ldy, nrhs, mode, dstatus, s, tiny);
     if (n <= 0 || nrhs <= 0) return RL_OK;
     const int nb = ceil_div(n, kSweepRows);
-    RL_LAUNCH((trsv_sweep_kernel<T, TA>), std::min(nb, kSweepCtas), 256, 0, s, A, lda, n, Y, ldy, nrhs, mode, ctl,
+    RL_LAUNCH((trsv_sweep_kernel<T, TA>), dim3(std::min(nb, kSweepCtas), sweep_groups(nrhs)), 256, 0, s, A, lda, n, Y,
+              ldy, nrhs, mode, ctl,
               dstatus, tiny, wait_ns(), (int)tune(RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK), Dinv);
     return RL_OK;
 }

@@ -55,19 +55,20 @@ inline rl_status colnorm_dev(const double *V, long long ldv, int n, int nrhs, un
 // once) and the sweep flags that use them: the form of RL_TUNE_MIXED_SWEEP_INV.
 struct SweepInv {
     const float *D1 = nullptr, *D2 = nullptr;
-    int *ctl = nullptr;  // 2 x (1 + blocks) words, zeroed before each pair of sweeps
+    int *ctl = nullptr;  // 2 x sweep_ctl_words(n, nrhs) words, zeroed before each pair of sweeps
 };
 
 // W <- M^-1 W with the FP32 factor (LU: ipiv swaps, unit L, U; Cholesky: L, L^T). No
 // absolute-epsilon rule here: only a pivot below FLT_MIN counts as singular. With inv.D1
-// set, the sweeps apply the diagonal blocks' inverses (few right-hand sides only).
+// set, the sweeps apply the diagonal blocks' inverses (up to kSweepGroups x kSweepRhs
+// right-hand sides).
 inline rl_status precond_solve(const float *F, int n, int kind, const int *ipiv, float *W, long long ldw, int nrhs,
                                int *dstatus, cudaStream_t s, const SweepInv &inv = SweepInv()) {
     const float tiny = FLT_MIN;
     const int m1 = kind == RL_KIND_LU ? 0 : 1, m2 = kind == RL_KIND_LU ? 2 : 3;
     if (kind == RL_KIND_LU) RL_TRY(laswp<float>(W, ldw, nrhs, 0, 0, ipiv, 0, n, s));
-    if (inv.D1 && nrhs <= kSweepRhs) {
-        const int words = 1 + ceil_div(n, kSweepRows);
+    if (inv.D1 && sweep_groups(nrhs) > 0) {
+        const int words = sweep_ctl_words(n, nrhs);
         RL_TRY_CUDA(cudaMemsetAsync(inv.ctl, 0, 2 * words * sizeof(int), s));
         RL_TRY((tri_solve_inv_dev<float, float>(F, n, n, inv.D1, W, ldw, nrhs, m1, dstatus, s, tiny, inv.ctl)));
         return tri_solve_inv_dev<float, float>(F, n, n, inv.D2, W, ldw, nrhs, m2, dstatus, s, tiny, inv.ctl + words);
@@ -440,9 +441,9 @@ struct MixedFactor {
         RL_TRY_CUDA(cudaMemsetAsync(dstatus.p, 0, 2 * sizeof(int), s));
         SweepInv inv;
         DevBuf<int> sweep_ctl;
-        if (tune(RL_TUNE_MIXED_SWEEP_INV) && nrhs <= kSweepRhs && n > CTA_NMAX) {
+        if (tune(RL_TUNE_MIXED_SWEEP_INV) && sweep_groups(nrhs) > 0 && n > CTA_NMAX && !g_shared_gpu) {
             RL_TRY(ensure_dinv(dstatus.p, s));
-            RL_TRY(sweep_ctl.alloc(2 * (size_t)(1 + ceil_div(n, kSweepRows)), s));
+            RL_TRY(sweep_ctl.alloc(2 * (size_t)sweep_ctl_words(n, nrhs), s));
             inv = SweepInv{Dinv, Dinv + dinv_elems(), sweep_ctl.p};
         }
         std::vector<int> act(nrhs + 1, 1);

@@ -66,11 +66,14 @@ def test_q_apply_shape_panics(gpu):
 
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
-@pytest.mark.parametrize("n,nrhs", [(1, 1), (37, 1), (300, 3), (1000, 1), (1000, 12), (2500, 5)])
+@pytest.mark.parametrize("n,nrhs", [(1, 1), (37, 1), (300, 3), (1000, 1), (1000, 12), (2500, 5), (700, 64),
+                                    (1100, 100), (600, 129)])
 def test_triangular_solves_against_oracle(gpu, dtype, n, nrhs):
     """solve_u_triangular / solve_l_triangular against the oracle's back_substitution /
     forward_substitution (src/matrix/mod.rs:318-398), column by column: backward error
-    within 10 n eps and the other triangle ignored (filled with NaN)."""
+    within 10 n eps and the other triangle ignored (filled with NaN). Up to 128
+    right-hand sides take the one-launch sweep in groups of 8 columns (100: a partial
+    last group), 129 the blocked path."""
     rng = np.random.default_rng(n + nrhs)
     t = rng.uniform(-1, 1, (n, n)) / np.sqrt(n) + np.diag(rng.uniform(1, 2, n))
     eps = U64 if dtype == np.float64 else U32
