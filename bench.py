@@ -765,9 +765,8 @@ def main():
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     alg_bytes = a_bytes + 2 * b_bytes
-    # DRAM traffic per launch from the committed ncu summary of this kernel (captured on a
-    # 6,000-system batch of the same mix and scaled there to 40,000 by matrix bytes);
-    # scaled here by matrix bytes to this run's batch.
+    # DRAM traffic per launch from the committed ncu summary of this kernel (one launch on
+    # a 6,000-system batch of the same mix), scaled here by matrix bytes to this batch.
     traffic = profile_traffic(a_bytes)
     fp64_peak = FP64_PEAK_TFLOPS
     fp64_floor_ms = fl64 / (fp64_peak * 1e12) * 1e3
