@@ -90,6 +90,8 @@ RL_API uint64_t rl_launch_count(void);
                                          precomputed inverse (a product) instead of a 64-step substitution:
                                          [0, 1], default 1 (1-7% faster at n = 4096-16384, same refinement
                                          steps within one) */
+#define RL_TUNE_PANEL_LOOKAHEAD 9     /* blocked LU panels on a cluster: column j + 1's pivot search and
+                                         push overlap the rest of column j's elimination: [0, 1], default 0 */
 #define RL_TUNE_TEST_WITHHOLD_CHUNK 100 /* tests only: the host batched path never sets this chunk's arrival
                                            flag, so its wait runs out (RL_ERR_TIMEOUT): [-1, 255], default -1 */
 #define RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK 101 /* tests only: the few-right-hand-side triangular sweep never

@@ -161,6 +161,7 @@ TUNE_UPLOAD_CHUNKS = 5
 TUNE_MIXED_REFINE_STEPS = 6
 TUNE_LU_OUTER_NB = 7
 TUNE_MIXED_SWEEP_INV = 8
+TUNE_PANEL_LOOKAHEAD = 9
 TUNE_TEST_WITHHOLD_CHUNK = 100
 TUNE_TEST_WITHHOLD_SWEEP_BLOCK = 101
 

@@ -400,6 +400,199 @@ static __global__ void __launch_bounds__(256) lu_panel_cluster_kernel(T *P, long
     cluster.sync();  // no CTA leaves while another may still read its shared memory
 }
 
+// The same panel with look-ahead across columns. After column j's winner is known a CTA
+// updates only column j + 1 of its rows, finds its candidate for column j + 1, completes
+// that candidate row (and row j + 1, if it holds it), pushes them and ARRIVES at the
+// cluster barrier; the rest of column j's elimination (columns j + 2 .. kb - 1 of its
+// other rows) runs while the barrier completes, and the CTA WAITS only before reading
+// column j + 1's records. Every element gets the same fma(-l, u, a) as in
+// lu_panel_cluster_kernel, so the factors and pivots are identical. The tables have three
+// slots: a CTA may push column j + 1 while another still eliminates with column j - 1's
+// pivot row.
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+
+template <class T>
+static __global__ void __launch_bounds__(256) lu_panel_cluster_la_kernel(T *P, long long lda, int mrows, int kb, int k0,
+                                                                  int rows_per, int tpr, int *ipiv, int *err, T tiny) {
+    namespace cg = cooperative_groups;
+    constexpr int NB = PanelNB<T>::value;
+    constexpr int LDR = NB + 1;
+    constexpr int CMAX = 16, NS = 3;
+    constexpr int VW = 16 / (int)sizeof(T);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *tab = reinterpret_cast<T *>(smem_raw);  // NS x CMAX x NB: every CTA's candidate row
+    T *rowj = tab + NS * CMAX * NB;            // NS x NB: row j (pushed by the CTA holding it)
+    T *R = rowj + NS * NB;                     // rows_per x LDR
+    __shared__ unsigned long long s_k[8], rec_k[NS * CMAX];
+    __shared__ int s_i[8], rec_i[NS * CMAX];
+    __shared__ T rec_inv[NS * CMAX];
+    cg::cluster_group cluster = cg::this_cluster();
+    const int C = (int)cluster.num_blocks(), g = (int)cluster.block_rank();
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int r0 = g * rows_per, r1 = min(mrows, r0 + rows_per), nr = max(0, r1 - r0);
+    const int q = tid & (tpr - 1), grp = tid / tpr, G = (int)blockDim.x / tpr;
+    const int rpt = (rows_per + G - 1) / G;
+    const unsigned long long ktiny = amax_key(tiny);
+    const int nch = (kb + VW - 1) / VW;
+    if (g == 0)
+        for (int j = tid; j < kb; j += blockDim.x) ipiv[j] = k0 + j;
+    for (int idx = tid; idx < nr * kb; idx += blockDim.x) {
+        const int r = idx / kb, c = idx - r * kb;
+        R[r * LDR + c] = P[(long long)(r0 + r) * lda + c];
+    }
+    __syncthreads();
+    // candidate of this CTA for column c (rows >= c; thread group q == c mod tpr scans)
+    auto candidate = [&](int c, unsigned long long &bk, int &bi) {
+        bk = 0ull;
+        bi = INT_MAX;
+        if (q == (c & (tpr - 1)))
+            for (int k = 0; k < rpt; k++) {
+                const int r = grp + k * G;
+                if (r < nr && r0 + r >= c) {
+                    const unsigned long long key = amax_key(R[r * LDR + c]);
+                    if (key > bk) {
+                        bk = key;
+                        bi = r0 + r;
+                    }
+                }
+            }
+        warp_amax_key<T>(bk, bi);
+        if (lane == 0) {
+            s_k[warp] = bk;
+            s_i[warp] = bi;
+        }
+        __syncthreads();
+        bk = s_k[0];
+        bi = s_i[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
+            const unsigned long long k2 = s_k[w];
+            const int i2 = s_i[w];
+            if (k2 > bk || (k2 == bk && i2 < bi)) {
+                bk = k2;
+                bi = i2;
+            }
+        }
+    };
+    // push the candidate row bi (complete) and row c (if held) into every CTA's slot for
+    // column c, with the record; then arrive
+    auto push = [&](int c, unsigned long long bk, int bi) {
+        const int slot = c % NS;
+        if (bk != 0ull)
+            for (int idx = tid; idx < C * nch; idx += blockDim.x) {
+                const int dst = idx / nch, ch = idx - dst * nch;
+                const T *src = R + (size_t)(bi - r0) * LDR + ch * VW;
+                uint4 v;
+                T *vt = reinterpret_cast<T *>(&v);
+#pragma unroll
+                for (int e = 0; e < VW; e++) vt[e] = src[e];
+                *reinterpret_cast<uint4 *>(cluster.map_shared_rank(tab + (slot * CMAX + g) * NB + ch * VW, dst)) = v;
+            }
+        if (c >= r0 && c < r1)
+            for (int idx = tid; idx < C * nch; idx += blockDim.x) {
+                const int dst = idx / nch, ch = idx - dst * nch;
+                const T *src = R + (size_t)(c - r0) * LDR + ch * VW;
+                uint4 v;
+                T *vt = reinterpret_cast<T *>(&v);
+#pragma unroll
+                for (int e = 0; e < VW; e++) vt[e] = src[e];
+                *reinterpret_cast<uint4 *>(cluster.map_shared_rank(rowj + slot * NB + ch * VW, dst)) = v;
+            }
+        if (warp == 0) {
+            const T inv = bk != 0ull ? T(1) / R[(bi - r0) * LDR + c] : T(0);
+            if (lane < C) {
+                const int e = slot * CMAX + g;
+                *cluster.map_shared_rank(rec_k + e, lane) = bk;
+                *cluster.map_shared_rank(rec_i + e, lane) = bk != 0ull ? bi : INT_MAX;
+                *cluster.map_shared_rank(rec_inv + e, lane) = inv;
+            }
+        }
+        cluster_arrive();
+    };
+    {
+        unsigned long long bk;
+        int bi;
+        candidate(0, bk, bi);
+        push(0, bk, bi);
+    }
+    int skip0 = -1, skip1 = -1;  // rows completed before their push (not eliminated again)
+    for (int j = 0; j < kb; j++) {
+        const int slot = j % NS, qj = j & (tpr - 1);
+        cluster_wait();  // column j's records and rows are in every CTA's tables
+        unsigned long long wk = lane < C ? rec_k[slot * CMAX + lane] : 0ull;
+        int wi = lane < C ? rec_i[slot * CMAX + lane] : INT_MAX;
+        warp_amax_key<T>(wk, wi);
+        int wg = -1;
+        if (wk != 0ull) {
+            if (wk < ktiny) {
+                if (g == 0 && tid == 0) atomicCAS(err, 0, RL_ERR_DIV_BY_ZERO);
+                break;
+            }
+            wg = wi / rows_per;
+        } else {
+            wi = j;
+        }
+        const T *oldj = rowj + slot * NB;
+        const T *prow = wg >= 0 ? tab + (slot * CMAX + wg) * NB : oldj;
+        if (g == 0 && tid == 0) ipiv[j] = k0 + wi;
+        const T inv_p = wg >= 0 ? rec_inv[slot * CMAX + wg] : T(1) / oldj[j];
+        if (wi != j && tid < kb) {
+            if (j >= r0 && j < r1) R[(j - r0) * LDR + tid] = prow[tid];
+            if (wi >= r0 && wi < r1 && tid < j) R[(wi - r0) * LDR + tid] = oldj[tid];
+        }
+        // (a) multipliers and column j + 1 of every row below j
+        const int q1 = (j + 1) & (tpr - 1);
+        for (int k = 0; k < rpt; k++) {
+            const int r = grp + k * G, gr = r0 + r;
+            const bool valid = r < nr && gr > j;
+            T *row = R + (size_t)(valid ? r : 0) * LDR;
+            const T *src = gr == wi ? oldj : row;
+            T l = T(0);
+            if (valid && q == qj) l = src[j] * inv_p;
+            if (tpr > 1) l = __shfl_sync(0xffffffffu, l, qj, tpr);
+            if (valid) {
+                if (q == qj) row[j] = l;
+                if (j + 1 < kb && q == q1) row[j + 1] = fma(-l, prow[j + 1], src[j + 1]);
+            }
+        }
+        if (j + 1 >= kb) break;
+        // (b) the candidate for column j + 1 (the barrier inside also orders (a))
+        unsigned long long bk;
+        int bi;
+        candidate(j + 1, bk, bi);
+        // (c) complete the rows pushed for column j + 1: the candidate and row j + 1
+        skip0 = bk != 0ull ? bi : -1;
+        skip1 = (j + 1 >= r0 && j + 1 < r1) ? j + 1 : -1;
+        for (int t = 0; t < 2; t++) {
+            const int gr = t == 0 ? skip0 : skip1;
+            if (gr < 0 || (t == 1 && gr == skip0)) continue;
+            T *row = R + (size_t)(gr - r0) * LDR;
+            const T *src = gr == wi ? oldj : row;
+            const T l = row[j];
+            for (int c = j + 2 + tid; c < kb; c += blockDim.x) row[c] = fma(-l, prow[c], src[c]);
+        }
+        __syncthreads();
+        push(j + 1, bk, bi);
+        // (d) the rest of column j's elimination, while the barrier completes
+        const int cfirst = j + 2 + ((q - j - 2) & (tpr - 1));
+        for (int k = 0; k < rpt; k++) {
+            const int r = grp + k * G, gr = r0 + r;
+            if (r >= nr || gr <= j || gr == skip0 || gr == skip1) continue;
+            T *row = R + (size_t)r * LDR;
+            const T *src = gr == wi ? oldj : row;
+            const T l = row[j];
+#pragma unroll 4
+            for (int c = cfirst; c < kb; c += tpr) row[c] = fma(-l, prow[c], src[c]);
+        }
+    }
+    __syncthreads();
+    for (int idx = tid; idx < nr * kb; idx += blockDim.x) {
+        const int r = idx / kb, c = idx - r * kb;
+        P[(long long)(r0 + r) * lda + c] = R[r * LDR + c];
+    }
+    cluster.sync();  // no CTA leaves while another may still read its shared memory
+}
+
 // ------------------------------------------------------------ Householder panel --
 // Unblocked Householder QR of the panel rows [0, mrows) x cols [0, kb) (P points at
 // A[k0][k0]), reflector by reflector exactly as HouseholderReflection::compute and

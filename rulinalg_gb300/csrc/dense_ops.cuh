@@ -135,10 +135,14 @@ rl_status lu_panel_cluster(T *P, long long lda, int mrows, int kb, int k0, int *
                            bool &launched) {
     constexpr int NB = PanelNB<T>::value;
     launched = false;
-    auto kern = lu_panel_cluster_kernel<T>;
-    static const int cmax_hw = probe_cluster(kern, kClusterSmem);
-    const int cmax = std::min<int>(cmax_hw, (int)tune(RL_TUNE_PANEL_CLUSTER_MAX));
-    const size_t row_bytes = (NB + 1) * sizeof(T), extra = (2 * 16 * NB + 2 * NB) * sizeof(T);
+    // look-ahead form (RL_TUNE_PANEL_LOOKAHEAD): three table slots instead of two
+    const bool la = tune(RL_TUNE_PANEL_LOOKAHEAD) != 0;
+    auto kern = la ? lu_panel_cluster_la_kernel<T> : lu_panel_cluster_kernel<T>;
+    static const int cmax_hw = probe_cluster(lu_panel_cluster_kernel<T>, kClusterSmem);
+    static const int cmax_hw_la = probe_cluster(lu_panel_cluster_la_kernel<T>, kClusterSmem);
+    const int cmax = std::min<int>(la ? cmax_hw_la : cmax_hw, (int)tune(RL_TUNE_PANEL_CLUSTER_MAX));
+    const int slots = la ? 3 : 2;
+    const size_t row_bytes = (NB + 1) * sizeof(T), extra = (slots * 16 * NB + slots * NB) * sizeof(T);
     int rows_per = 0;
     const int C = cluster_shape(mrows, row_bytes, extra, cmax, panel_target_rows<T>(), rows_per);
     if (C == 0) return RL_OK;

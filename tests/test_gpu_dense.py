@@ -466,3 +466,31 @@ def test_lu_and_qr_cooperative_panels(gpu, dtype):
     assert fro(np.triu(h.qr.astype(np.float64))[:n_qr] - np.triu(oqr)[:n_qr]) <= 10 * n_qr * eps * fro(aq)
     lu2 = gpu.PartialPivLu.decompose(a)  # default: cluster panels
     assert np.array_equal(lu2.p.perm, operm)
+
+
+@pytest.mark.parametrize("dtype,n", [(np.float64, 700), (np.float64, 2000), (np.float64, 7000), (np.float32, 1500),
+                                     (np.float32, 4096)])
+def test_lu_panel_lookahead_bit_identical(gpu, dtype, n):
+    """RL_TUNE_PANEL_LOOKAHEAD = 1 overlaps the rest of column j's elimination with column
+    j + 1's pivot search and push (cluster panels); every element gets the same
+    fma(-l, u, a), so the factors and the permutation are bit-identical to the plain
+    panel's (n = 7000 f64: the first panels are too tall for a cluster and run on the
+    cooperative kernel, the later ones on the cluster). A mixed-precision solve with it
+    stays f64-accurate."""
+    from rulinalg_gb300 import _lib as L
+    rng = np.random.default_rng(n)
+    a = (rng.uniform(-1, 1, (n, n)) + np.eye(n)).astype(dtype)
+    saved = gpu.tune_get(L.TUNE_PANEL_LOOKAHEAD)
+    try:
+        gpu.tune_set(L.TUNE_PANEL_LOOKAHEAD, 0)
+        plain = gpu.PartialPivLu.decompose(a)
+        gpu.tune_set(L.TUNE_PANEL_LOOKAHEAD, 1)
+        la = gpu.PartialPivLu.decompose(a)
+        if dtype == np.float64 and n <= 2000:
+            b = rng.standard_normal(n)
+            x, info = gpu.solve_mixed(a, b, "lu")
+            assert backward_error(a, x, b) <= n * U64 * 10, info
+    finally:
+        gpu.tune_set(L.TUNE_PANEL_LOOKAHEAD, saved)
+    assert np.array_equal(la.p.perm, plain.p.perm)
+    assert np.array_equal(la.lu.view(np.uint8), plain.lu.view(np.uint8))
