@@ -91,7 +91,8 @@ RL_API uint64_t rl_launch_count(void);
                                          [0, 1], default 1 (1-7% faster at n = 4096-16384, same refinement
                                          steps within one) */
 #define RL_TUNE_PANEL_LOOKAHEAD 9     /* blocked LU panels on a cluster: column j + 1's pivot search and
-                                         push overlap the rest of column j's elimination: [0, 1], default 0 */
+                                         push overlap the rest of column j's elimination (bit-identical
+                                         factors; measured not faster on GB300): [0, 1], default 0 */
 #define RL_TUNE_TEST_WITHHOLD_CHUNK 100 /* tests only: the host batched path never sets this chunk's arrival
                                            flag, so its wait runs out (RL_ERR_TIMEOUT): [-1, 255], default -1 */
 #define RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK 101 /* tests only: the few-right-hand-side triangular sweep never
