@@ -344,7 +344,7 @@ def test_cholesky_golden(gpu, golden):
         assert_matrix_float_eq(gpu.Cholesky.decompose(np.eye(n)).unpack(), np.eye(n))
 
 
-@pytest.mark.parametrize("n", [1, 3, 16, 33, 64, 100, 257, 512, 513, 700])
+@pytest.mark.parametrize("n", [1, 3, 16, 33, 64, 100, 257, 512, 513, 700, 1500, 2500])
 def test_cholesky_parity_random(gpu, n):
     rng = np.random.default_rng(100 + n)
     g = rng.standard_normal((n, n))
@@ -360,6 +360,28 @@ def test_cholesky_parity_random(gpu, n):
     x = ch.solve(b)
     assert backward_error(a, x, b) <= n * U64 * 10
     assert ch.det() == pytest.approx(O.chol_det(ol), rel=1e-10)
+
+
+@pytest.mark.parametrize("n", [513, 1100, 2500])
+def test_cholesky_f32_blocked_against_f64_oracle(gpu, n):
+    """Matrix<f32> Cholesky above one CTA's size: 256-column outer blocks whose L21 and
+    SYRK run on the tensor cores (3xTF32). Against the f64 oracle's factor of the same
+    (f32-rounded) matrix: reconstruction and factor within 10 n u32 (A = G G^T / n + I,
+    condition number below 10), strict upper triangle untouched."""
+    rng = np.random.default_rng(300 + n)
+    g = rng.standard_normal((n, n))
+    a32 = (g @ g.T / n + np.eye(n)).astype(np.float32)
+    given = a32.copy()
+    given[np.triu_indices(n, 1)] = np.nan
+    ch = gpu.Cholesky.decompose(given)
+    assert np.isnan(ch.l[np.triu_indices(n, 1)]).all()
+    l = np.tril(ch.l).astype(np.float64)
+    a = a32.astype(np.float64)
+    ol, st = O.chol_decompose(a)
+    assert st == O.OK
+    u32 = 2.0 ** -24
+    assert fro(l @ l.T - a) <= 10 * n * u32 * fro(a)
+    assert fro(l - np.tril(ol)) <= 10 * n * u32 * fro(np.tril(ol))
 
 
 # ---------------------------------------------------------------- Householder --
