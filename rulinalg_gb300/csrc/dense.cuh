@@ -1014,10 +1014,11 @@ static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const TA *__rest
                                                              unsigned long long wait_ns, int withhold,
                                                              const T *__restrict__ Dinv) {
     constexpr int BR = kSweepRows, LDD = BR + 1;
-    __shared__ T Ds[BR * LDD];           // the diagonal block
-    __shared__ T inv[BR];                 // 1 / d_ii
-    __shared__ T xs[BR * kSweepRhs];      // a published block's solution, then the folded sums
-    __shared__ int s_t, s_fail;
+    constexpr int FB = sizeof(T) == 4 ? 8 : 2;  // published blocks folded per barrier round
+    __shared__ T Ds[BR * LDD];                  // the diagonal block
+    __shared__ T inv[BR];                        // 1 / d_ii
+    __shared__ T xs[FB * BR * kSweepRhs];        // a round's published solutions, then the folded sums
+    __shared__ int s_t, s_fail, s_m;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nb = (n + BR - 1) / BR;
     const bool fwd = mode <= 1, trans = mode == 3;
@@ -1051,17 +1052,15 @@ static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const TA *__rest
     #pragma unroll
         for (int c = 0; c < kSweepRhs; c++) acc[c] = T(0);
         const int nk = fwd ? b : nb - 1 - b;  // blocks solved before this one
-        for (int kk = 0; kk < nk; kk++) {
-            const int k = fwd ? kk : nb - 1 - kk, c0 = k * BR, ks = min(BR, n - c0);
-            T a[16];
-    #pragma unroll
-            for (int jj = 0; jj < 16; jj++) {
-                const int j = q * 16 + jj;
-                a[jj] = (r < bs && j < ks)
-                            ? T(trans ? A[(long long)(c0 + j) * lda + r0 + r] : A[(long long)(r0 + r) * lda + c0 + j])
-                            : T(0);
-            }
+        // The fold, in rounds of up to FB published blocks: thread 0 waits (bounded) for the
+        // round's first block and takes the consecutive published ones after it; their
+        // solutions go to shared memory under one barrier, and the round's products run
+        // without barriers between blocks. (One block per round cost three barriers and a
+        // dependent memory round trip per earlier block: O(b) latencies for block b.) Each
+        // thread adds the blocks in the same order as before, so the sums are unchanged.
+        for (int kk0 = 0; kk0 < nk;) {
             if (tid == 0 && !s_fail) {
+                const int k = fwd ? kk0 : nb - 1 - kk0;
                 const unsigned long long t0 = global_ns();
                 while (ld_acquire(ctl + 1 + k) == 0) {
                     if (global_ns() - t0 > wait_ns) {
@@ -1070,24 +1069,44 @@ static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const TA *__rest
                     }
                     __nanosleep(100);
                 }
+                int m = 1;
+                while (!s_fail && m < FB && kk0 + m < nk &&
+                       ld_acquire(ctl + 1 + (fwd ? kk0 + m : nb - 1 - (kk0 + m))) != 0)
+                    m++;
+                s_m = m;
             }
             __syncthreads();
             if (s_fail) break;
+            const int m = s_m;
             // rows ks..BR-1 of a short last block are zeroed: they meet a[jj] = 0, and a
             // stale shared value there could be a NaN (0 * NaN = NaN)
-            for (int idx = tid; idx < BR * nrhs; idx += blockDim.x) {
-                const int i = idx / nrhs, c = idx - i * nrhs;
-                xs[i * kSweepRhs + c] = i < ks ? __ldcg(Y + (long long)(c0 + i) * ldy + c) : T(0);
+            for (int idx = tid; idx < m * BR * nrhs; idx += blockDim.x) {
+                const int u = idx / (BR * nrhs), rem = idx - u * (BR * nrhs), i = rem / nrhs, c = rem - i * nrhs;
+                const int k = fwd ? kk0 + u : nb - 1 - (kk0 + u), c0 = k * BR, ks = min(BR, n - c0);
+                xs[(u * BR + i) * kSweepRhs + c] = i < ks ? __ldcg(Y + (long long)(c0 + i) * ldy + c) : T(0);
             }
             __syncthreads();
+    #pragma unroll 2
+            for (int u = 0; u < m; u++) {
+                const int k = fwd ? kk0 + u : nb - 1 - (kk0 + u), c0 = k * BR, ks = min(BR, n - c0);
+                T a[16];
     #pragma unroll
-            for (int jj = 0; jj < 16; jj++) {
-                const int j = q * 16 + jj;
+                for (int jj = 0; jj < 16; jj++) {
+                    const int j = q * 16 + jj;
+                    a[jj] = (r < bs && j < ks)
+                                ? T(trans ? A[(long long)(c0 + j) * lda + r0 + r] : A[(long long)(r0 + r) * lda + c0 + j])
+                                : T(0);
+                }
     #pragma unroll
-                for (int c = 0; c < kSweepRhs; c++)
-                    if (c < nrhs) acc[c] = fma(a[jj], xs[j * kSweepRhs + c], acc[c]);
+                for (int jj = 0; jj < 16; jj++) {
+                    const int j = q * 16 + jj;
+    #pragma unroll
+                    for (int c = 0; c < kSweepRhs; c++)
+                        if (c < nrhs) acc[c] = fma(a[jj], xs[(u * BR + j) * kSweepRhs + c], acc[c]);
+                }
             }
-            __syncthreads();  // xs is refilled for the next block
+            __syncthreads();  // xs is refilled by the next round
+            kk0 += m;
         }
         // sum of the 4 column quarters of each row into xs
         if (!trans) {
