@@ -1007,7 +1007,7 @@ inline int sweep_groups(int nrhs) {
 inline int sweep_ctl_words(int n, int nrhs) {
     return sweep_groups(nrhs) * (1 + (n + kSweepRows - 1) / kSweepRows);
 }
-template <class T, class TA = T>
+template <class T, class TA = T, int RW = kSweepRhs>
 static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const TA *__restrict__ A, long long lda, int n,
                                                              T *__restrict__ Y, long long ldy, int nrhs, int mode,
                                                              int *ctl, int *status, T tiny,
@@ -1048,9 +1048,9 @@ static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const TA *__rest
         // thread (row r, quarter q): non-transposed reads A[r][q * 16 + jj] (a thread's 16
         // columns contiguous), transposed reads A[q * 16 + jj][r] (a warp's rows contiguous)
         const int r = trans ? (tid & (BR - 1)) : (tid >> 2), q = trans ? (tid >> 6) : (tid & 3);
-        T acc[kSweepRhs];
+        T acc[RW];
     #pragma unroll
-        for (int c = 0; c < kSweepRhs; c++) acc[c] = T(0);
+        for (int c = 0; c < RW; c++) acc[c] = T(0);
         const int nk = fwd ? b : nb - 1 - b;  // blocks solved before this one
         // The fold, in rounds of up to FB published blocks: thread 0 waits (bounded) for the
         // round's first block and takes the consecutive published ones after it; their
@@ -1101,7 +1101,7 @@ static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const TA *__rest
                 for (int jj = 0; jj < 16; jj++) {
                     const int j = q * 16 + jj;
     #pragma unroll
-                    for (int c = 0; c < kSweepRhs; c++)
+                    for (int c = 0; c < RW; c++)
                         if (c < nrhs) acc[c] = fma(a[jj], xs[(u * BR + j) * kSweepRhs + c], acc[c]);
                 }
             }
@@ -1111,19 +1111,19 @@ static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const TA *__rest
         // sum of the 4 column quarters of each row into xs
         if (!trans) {
     #pragma unroll
-            for (int c = 0; c < kSweepRhs; c++) {
+            for (int c = 0; c < RW; c++) {
                 acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 1);
                 acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 2);
             }
             if (q == 0)
     #pragma unroll
-                for (int c = 0; c < kSweepRhs; c++) xs[r * kSweepRhs + c] = acc[c];
+                for (int c = 0; c < RW; c++) xs[r * kSweepRhs + c] = acc[c];
             __syncthreads();
         } else {
             for (int qq = 0; qq < 4; qq++) {
                 if (q == qq)
     #pragma unroll
-                    for (int c = 0; c < kSweepRhs; c++) xs[r * kSweepRhs + c] = (qq ? xs[r * kSweepRhs + c] : T(0)) + acc[c];
+                    for (int c = 0; c < RW; c++) xs[r * kSweepRhs + c] = (qq ? xs[r * kSweepRhs + c] : T(0)) + acc[c];
                 __syncthreads();
             }
         }
@@ -1136,24 +1136,26 @@ static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const TA *__rest
             __syncthreads();
             const int rr = tid >> 2, qq = tid & 3;
             const T *Db = Dinv + (long long)b * BR * BR + (long long)rr * BR + qq * 16;
-            T xo[kSweepRhs];
+            T xo[RW];
     #pragma unroll
-            for (int c = 0; c < kSweepRhs; c++) xo[c] = T(0);
+            for (int c = 0; c < RW; c++) xo[c] = T(0);
     #pragma unroll
             for (int jj = 0; jj < 16; jj++) {
                 const int j = qq * 16 + jj;
                 const T dv = (rr < bs && j < bs) ? Db[jj] : T(0);
     #pragma unroll
-                for (int c = 0; c < kSweepRhs; c++)
+                for (int c = 0; c < RW; c++)
                     if (c < nrhs) xo[c] = fma(dv, xs[j * kSweepRhs + c], xo[c]);
             }
     #pragma unroll
-            for (int c = 0; c < kSweepRhs; c++) {
+            for (int c = 0; c < RW; c++) {
                 xo[c] += __shfl_xor_sync(0xffffffffu, xo[c], 1);
                 xo[c] += __shfl_xor_sync(0xffffffffu, xo[c], 2);
             }
             if (qq == 0 && rr < bs && !s_fail)
-                for (int c = 0; c < nrhs; c++) __stcg(Y + (long long)(r0 + rr) * ldy + c, xo[c]);
+    #pragma unroll
+                for (int c = 0; c < RW; c++)
+                    if (c < nrhs) __stcg(Y + (long long)(r0 + rr) * ldy + c, xo[c]);
         }
         // substitution: warp c solves right-hand side c; lane l holds rows l and l + 32
         if (!Dinv && warp < nrhs && !s_fail) {

@@ -512,9 +512,15 @@ rl_status tri_solve_dev(const TA *A, long long lda, int n, T *Y, long long ldy, 
         DevBuf<int> ctl;
         RL_TRY(ctl.alloc(words, s));
         RL_TRY_CUDA(cudaMemsetAsync(ctl.p, 0, sizeof(int) * words, s));
-        RL_LAUNCH((trsv_sweep_kernel<T, TA>), dim3(std::min(nb, kSweepCtas), sweep_groups(nrhs)), 256, 0, s, A, lda, n, Y,
-                  ldy, nrhs, mode, ctl.p, dstatus, tiny, wait_ns(), (int)tune(RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK),
-                  (const T *)nullptr);
+        // one right-hand side: the 1-wide instance (the 8-wide one would issue 8 FMAs per
+        // element, 7 of them predicated off, each a full issue of the FP64 pipe for T = double)
+        const dim3 grid(std::min(nb, kSweepCtas), sweep_groups(nrhs));
+        if (nrhs == 1)
+            RL_LAUNCH((trsv_sweep_kernel<T, TA, 1>), grid, 256, 0, s, A, lda, n, Y, ldy, nrhs, mode, ctl.p, dstatus, tiny,
+                      wait_ns(), (int)tune(RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK), (const T *)nullptr);
+        else
+            RL_LAUNCH((trsv_sweep_kernel<T, TA>), grid, 256, 0, s, A, lda, n, Y, ldy, nrhs, mode, ctl.p, dstatus, tiny,
+                      wait_ns(), (int)tune(RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK), (const T *)nullptr);
         return RL_OK;
     }
     if constexpr (!std::is_same<T, TA>::value) {
@@ -573,9 +579,13 @@ rl_status tri_solve_inv_dev(const TA *A, long long lda, int n, const T *Dinv, T 
         return tri_solve_dev<T, TA>(A, lda, n, Y, ldy, nrhs, mode, dstatus, s, tiny);
     if (n <= 0 || nrhs <= 0) return RL_OK;
     const int nb = ceil_div(n, kSweepRows);
-    RL_LAUNCH((trsv_sweep_kernel<T, TA>), dim3(std::min(nb, kSweepCtas), sweep_groups(nrhs)), 256, 0, s, A, lda, n, Y,
-              ldy, nrhs, mode, ctl,
-              dstatus, tiny, wait_ns(), (int)tune(RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK), Dinv);
+    const dim3 grid(std::min(nb, kSweepCtas), sweep_groups(nrhs));
+    if (nrhs == 1)
+        RL_LAUNCH((trsv_sweep_kernel<T, TA, 1>), grid, 256, 0, s, A, lda, n, Y, ldy, nrhs, mode, ctl, dstatus, tiny,
+                  wait_ns(), (int)tune(RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK), Dinv);
+    else
+        RL_LAUNCH((trsv_sweep_kernel<T, TA>), grid, 256, 0, s, A, lda, n, Y, ldy, nrhs, mode, ctl, dstatus, tiny,
+                  wait_ns(), (int)tune(RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK), Dinv);
     return RL_OK;
 }
 

@@ -59,16 +59,29 @@ static __global__ void residual_gemv_kernel(const double *__restrict__ A, long l
         double s[NR];
 #pragma unroll
         for (int c = 0; c < NR; c++) s[c] = 0.0;
-        for (int j = lane; j < n; j += 32) {
-            const double a = row[j];
+        // 8 columns' loads issued before their DFMAs (the same DFMAs, in the same order)
+        for (int j0 = lane; j0 < n; j0 += 32 * 8) {
+            double a[8], xv[8][NR];
 #pragma unroll
-            for (int c = 0; c < NR; c++)
-                if (c < nrhs) s[c] = fma(a, X[(long long)j * ldx + c], s[c]);
+            for (int u = 0; u < 8; u++) {
+                const int j = j0 + 32 * u;
+                a[u] = j < n ? row[j] : 0.0;
+#pragma unroll
+                for (int c = 0; c < NR; c++) xv[u][c] = (j < n && c < nrhs) ? X[(long long)j * ldx + c] : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++)
+                if (j0 + 32 * u < n)
+#pragma unroll
+                    for (int c = 0; c < NR; c++)
+                        if (c < nrhs) s[c] = fma(a[u], xv[u][c], s[c]);
         }
 #pragma unroll
         for (int c = 0; c < NR; c++) s[c] = warp_sum(s[c]);
         if (lane == 0)
-            for (int c = 0; c < nrhs; c++) R[(long long)i * ldr + c] = B ? B[(long long)i * ldb + c] - s[c] : s[c];
+#pragma unroll
+            for (int c = 0; c < NR; c++)
+                if (c < nrhs) R[(long long)i * ldr + c] = B ? B[(long long)i * ldb + c] - s[c] : s[c];
     }
 }
 

@@ -35,7 +35,15 @@ inline double bits_to_double(unsigned long long b) {
 inline rl_status residual_dev(const double *A, long long lda, int n, const double *X, long long ldx, const double *B,
                        long long ldb, double *R, long long ldr, int nrhs, cudaStream_t s) {
     if (nrhs <= 4) {
-        RL_LAUNCH(residual_gemv_kernel<4>, grid_rows(n, 8), 256, 0, s, A, lda, n, X, ldx, B, ldb, R, ldr, nrhs);
+        // instantiated for the exact count: the FP64 pipe spends its ~64 cycles on a warp
+        // DFMA whose predicate is off as well, so a 4-column instance on one column costs 4x
+        const int g = grid_rows(n, 8);
+        if (nrhs == 1)
+            RL_LAUNCH(residual_gemv_kernel<1>, g, 256, 0, s, A, lda, n, X, ldx, B, ldb, R, ldr, nrhs);
+        else if (nrhs == 2)
+            RL_LAUNCH(residual_gemv_kernel<2>, g, 256, 0, s, A, lda, n, X, ldx, B, ldb, R, ldr, nrhs);
+        else
+            RL_LAUNCH(residual_gemv_kernel<4>, g, 256, 0, s, A, lda, n, X, ldx, B, ldb, R, ldr, nrhs);
         return RL_OK;
     }
     if (B)
