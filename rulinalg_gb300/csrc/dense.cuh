@@ -1033,6 +1033,27 @@ static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const TA *__rest
         __syncthreads();
         if (s_t >= nb) break;
         const int b = fwd ? s_t : nb - 1 - s_t, r0 = b * BR, bs = min(BR, n - r0);
+        // Loads that do not wait on other blocks, issued before the fold: this block's
+        // right-hand-side rows (only this block writes them) and, with Dinv, its row of
+        // the inverted diagonal block; first read after the fold, off the chain.
+        const int rr = tid >> 2, qq = tid & 3;
+        T dpre[16], ypre[2];
+        if (Dinv) {
+            const T *Db = Dinv + (long long)b * BR * BR + (long long)rr * BR + qq * 16;
+    #pragma unroll
+            for (int jj = 0; jj < 16; jj++) dpre[jj] = (rr < bs && qq * 16 + jj < bs) ? Db[jj] : T(0);
+    #pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int idx = tid + h * 256, i = idx / nrhs, c = idx - i * nrhs;
+                ypre[h] = idx < bs * nrhs ? __ldcg(Y + (long long)(r0 + i) * ldy + c) : T(0);
+            }
+        } else {
+    #pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int i = lane + 32 * h;
+                ypre[h] = (warp < nrhs && i < bs) ? __ldcg(Y + (long long)(r0 + i) * ldy + warp) : T(0);
+            }
+        }
         // the diagonal block and its reciprocal diagonal: no dependence on other blocks
         if (!Dinv)
             for (int idx = tid; idx < bs * bs; idx += blockDim.x) {
@@ -1129,23 +1150,21 @@ static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const TA *__rest
         }
         if (Dinv) {
             // x_b = Dinv_b v, v = y_b - folded sums (in xs); thread (row rr, quarter qq)
-            for (int idx = tid; idx < bs * nrhs; idx += blockDim.x) {
-                const int i = idx / nrhs, c = idx - i * nrhs;
-                xs[i * kSweepRhs + c] = __ldcg(Y + (long long)(r0 + i) * ldy + c) - xs[i * kSweepRhs + c];
+    #pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int idx = tid + h * 256, i = idx / nrhs, c = idx - i * nrhs;
+                if (idx < bs * nrhs) xs[i * kSweepRhs + c] = ypre[h] - xs[i * kSweepRhs + c];
             }
             __syncthreads();
-            const int rr = tid >> 2, qq = tid & 3;
-            const T *Db = Dinv + (long long)b * BR * BR + (long long)rr * BR + qq * 16;
             T xo[RW];
     #pragma unroll
             for (int c = 0; c < RW; c++) xo[c] = T(0);
     #pragma unroll
             for (int jj = 0; jj < 16; jj++) {
                 const int j = qq * 16 + jj;
-                const T dv = (rr < bs && j < bs) ? Db[jj] : T(0);
     #pragma unroll
                 for (int c = 0; c < RW; c++)
-                    if (c < nrhs) xo[c] = fma(dv, xs[j * kSweepRhs + c], xo[c]);
+                    if (c < nrhs) xo[c] = fma(dpre[jj], xs[j * kSweepRhs + c], xo[c]);
             }
     #pragma unroll
             for (int c = 0; c < RW; c++) {
@@ -1165,7 +1184,7 @@ static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const TA *__rest
             for (int h = 0; h < 2; h++) {
                 const int i = lane + 32 * h;
                 T v = T(0);
-                if (i < bs) v = __ldcg(Y + (long long)(r0 + i) * ldy + c) - xs[i * kSweepRhs + c];
+                if (i < bs) v = ypre[h] - xs[i * kSweepRhs + c];
                 y[h] = v;
             }
             if (fwd) {

@@ -1057,13 +1057,16 @@ __device__ double residual_rows(const TI *__restrict__ A, int lda, const TI *__r
         const double bl = mine < n ? (double)b[mine] : 0.0;
         double s[R];
 #pragma unroll
-        for (int r = 0; r < R; r++) {
-            s[r] = 0.0;
+        for (int r = 0; r < R; r++) s[r] = 0.0;
+        // chunk by chunk, each row's terms in the same order; the chunks at or past n are
+        // left by a warp-uniform branch (a predicated-off DFMA still takes the FP64 pipe)
 #pragma unroll
-            for (int c = 0; c < C; c++) {
-                const int j = lane + 32 * c;
-                if (32 * c < n) s[r] = fma((double)v[r][c], j < n ? S.x()[j] : 0.0, s[r]);
-            }
+        for (int c = 0; c < C; c++) {
+            if (32 * c >= n) break;
+            const int j = lane + 32 * c;
+            const double xj = j < n ? S.x()[j] : 0.0;
+#pragma unroll
+            for (int r = 0; r < R; r++) s[r] = fma((double)v[r][c], xj, s[r]);
         }
         // the rows' warp sums with R - 1 + 5 - log2 R FP64 additions (a warp-wide FP64
         // instruction is tens of cycles of the SM's FP64 pipe on this part)
