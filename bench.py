@@ -733,6 +733,14 @@ def main():
         for _ in range(max(1, args.warmup)):
             assert rl.lib.rl_dbatch_solve(*args_c) == 0
         torch.cuda.synchronize()
+        # this host's pinned host-to-device rate for the same buffer (one plain copy),
+        # which bounds the end-to-end step (the upload is overlapped with the solve)
+        dst = torch.empty_like(a)
+        t0 = time.perf_counter()
+        dst.copy_(a_h, non_blocking=True)
+        torch.cuda.synchronize()
+        h2d_gbs = a_bytes / (time.perf_counter() - t0) / 1e9
+        del dst
         ts = []
         for _ in range(args.steps):
             t0 = time.perf_counter()
@@ -744,6 +752,7 @@ def main():
                "h2d_bytes_per_step": int(a_bytes + b_bytes),
                "d2h_bytes_per_step": int(b_bytes + count * (4 + 4 + 8)),
                "ms_steps": [round(1e3 * t, 2) for t in ts], "host_affinity": affinity,
+               "h2d_gbs_pinned": h2d_gbs, "upload_ms_at_that_rate": 1e3 * (a_bytes + b_bytes) / (h2d_gbs * 1e9),
                "timing": "host clock around each rl_dbatch_solve call (pinned host buffers in, results out)"}
         assert np.array_equal(x_h.numpy(), mixed["x"].cpu().numpy()), "host and device entry points disagree"
 
