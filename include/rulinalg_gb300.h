@@ -93,6 +93,8 @@ RL_API uint64_t rl_launch_count(void);
 #define RL_TUNE_PANEL_LOOKAHEAD 9     /* blocked LU panels on a cluster: column j + 1's pivot search and
                                          push overlap the rest of column j's elimination (bit-identical
                                          factors; measured not faster on GB300): [0, 1], default 0 */
+#define RL_TUNE_FULLPIV_CTAS_PER_SM 10 /* FullPivLu's cooperative launch: CTAs per SM, [1, 3], default 3 (each
+                                          elimination step ends in a grid barrier over all of them) */
 #define RL_TUNE_TEST_WITHHOLD_CHUNK 100 /* tests only: the host batched path never sets this chunk's arrival
                                            flag, so its wait runs out (RL_ERR_TIMEOUT): [-1, 255], default -1 */
 #define RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK 101 /* tests only: the few-right-hand-side triangular sweep never

@@ -162,6 +162,7 @@ TUNE_MIXED_REFINE_STEPS = 6
 TUNE_LU_OUTER_NB = 7
 TUNE_MIXED_SWEEP_INV = 8
 TUNE_PANEL_LOOKAHEAD = 9
+TUNE_FULLPIV_CTAS_PER_SM = 10
 TUNE_TEST_WITHHOLD_CHUNK = 100
 TUNE_TEST_WITHHOLD_SWEEP_BLOCK = 101
 

@@ -246,10 +246,12 @@ rl_status full_lu_dev(T *A, long long lda, int n, int *piv_r, int *piv_c, int &s
     int per_sm = 0;
     RL_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFpThreads, 0));
     const long long want = ((long long)n * n + 8LL * kFpThreads - 1) / (8LL * kFpThreads);
-    // at most 3 CTAs per SM: each step ends in a grid barrier and reads every CTA's
-    // candidate, and the elimination is bound by the FP64 pipe, not by loads in flight
+    // at most RL_TUNE_FULLPIV_CTAS_PER_SM (3) CTAs per SM: each step ends in a grid
+    // barrier and reads every CTA's candidate, and the elimination is bound by the FP64
+    // pipe, not by loads in flight
+    const int cap = (int)tune(RL_TUNE_FULLPIV_CTAS_PER_SM);
     const int G = (int)std::max<long long>(
-        1, std::min<long long>(want, (long long)std::max(1, std::min(per_sm, 3)) * num_sms()));
+        1, std::min<long long>(want, (long long)std::max(1, std::min(per_sm, cap)) * num_sms()));
     DevBuf<T> W0, W1;
     DevBuf<unsigned long long> cv;
     DevBuf<long long> ci;

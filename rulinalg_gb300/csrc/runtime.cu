@@ -81,6 +81,7 @@ TuneKey g_tune_keys[] = {
     {RL_TUNE_LU_OUTER_NB, -1, 4096, -1},
     {RL_TUNE_MIXED_SWEEP_INV, 0, 1, 1},
     {RL_TUNE_PANEL_LOOKAHEAD, 0, 1, 0},
+    {RL_TUNE_FULLPIV_CTAS_PER_SM, 1, 3, 3},
     {RL_TUNE_TEST_WITHHOLD_CHUNK, -1, 255, -1},
     {RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK, -1, 1LL << 30, -1},
 };

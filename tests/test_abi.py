@@ -62,7 +62,7 @@ def test_tunables_ranges_and_defaults(rl):
     from rulinalg_gb300 import _lib as L
     defaults = {L.TUNE_WAIT_TIMEOUT_NS: 10 ** 9, L.TUNE_PANEL_CLUSTER_MAX: 16, L.TUNE_BATCH_CTAS_PER_SM: 0,
                 L.TUNE_BATCH_WARP_COST: 32768, L.TUNE_UPLOAD_CHUNKS: 32, L.TUNE_MIXED_REFINE_STEPS: 30,
-                L.TUNE_LU_OUTER_NB: -1, L.TUNE_MIXED_SWEEP_INV: 1, L.TUNE_PANEL_LOOKAHEAD: 0, L.TUNE_TEST_WITHHOLD_CHUNK: -1,
+                L.TUNE_LU_OUTER_NB: -1, L.TUNE_MIXED_SWEEP_INV: 1, L.TUNE_PANEL_LOOKAHEAD: 0, L.TUNE_FULLPIV_CTAS_PER_SM: 3, L.TUNE_TEST_WITHHOLD_CHUNK: -1,
                 L.TUNE_TEST_WITHHOLD_SWEEP_BLOCK: -1}
     for k, v in defaults.items():
         assert rl.tune_get(k) == v
