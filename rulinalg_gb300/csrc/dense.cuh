@@ -1080,6 +1080,19 @@ static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const TA *__rest
         // dependent memory round trip per earlier block: O(b) latencies for block b.) Each
         // thread adds the blocks in the same order as before, so the sums are unchanged.
         for (int kk0 = 0; kk0 < nk;) {
+            // FP32: the A tile of the block about to be waited for is loaded before the wait
+            constexpr bool PRE = sizeof(T) == 4;
+            T apre[PRE ? 16 : 1];
+            if (PRE) {
+                const int k = fwd ? kk0 : nb - 1 - kk0, c0 = k * BR, ks = min(BR, n - c0);
+    #pragma unroll
+                for (int jj = 0; jj < (PRE ? 16 : 1); jj++) {
+                    const int j = q * 16 + jj;
+                    apre[jj] = (r < bs && j < ks)
+                                   ? T(trans ? A[(long long)(c0 + j) * lda + r0 + r] : A[(long long)(r0 + r) * lda + c0 + j])
+                                   : T(0);
+                }
+            }
             if (tid == 0 && !s_fail) {
                 const int k = fwd ? kk0 : nb - 1 - kk0;
                 const unsigned long long t0 = global_ns();
@@ -1114,9 +1127,12 @@ static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const TA *__rest
     #pragma unroll
                 for (int jj = 0; jj < 16; jj++) {
                     const int j = q * 16 + jj;
-                    a[jj] = (r < bs && j < ks)
-                                ? T(trans ? A[(long long)(c0 + j) * lda + r0 + r] : A[(long long)(r0 + r) * lda + c0 + j])
-                                : T(0);
+                    if (PRE && u == 0)
+                        a[jj] = apre[PRE ? jj : 0];
+                    else
+                        a[jj] = (r < bs && j < ks)
+                                    ? T(trans ? A[(long long)(c0 + j) * lda + r0 + r] : A[(long long)(r0 + r) * lda + c0 + j])
+                                    : T(0);
                 }
     #pragma unroll
                 for (int jj = 0; jj < 16; jj++) {
