@@ -1080,8 +1080,9 @@ static __global__ void __launch_bounds__(256) trsv_sweep_kernel(const TA *__rest
         // dependent memory round trip per earlier block: O(b) latencies for block b.) Each
         // thread adds the blocks in the same order as before, so the sums are unchanged.
         for (int kk0 = 0; kk0 < nk;) {
-            // FP32: the A tile of the block about to be waited for is loaded before the wait
-            constexpr bool PRE = sizeof(T) == 4;
+            // FP32, one right-hand side: the A tile of the block about to be waited for is
+            // loaded before the wait (with 8 right-hand sides the extra registers cost more)
+            constexpr bool PRE = sizeof(T) == 4 && RW == 1;
             T apre[PRE ? 16 : 1];
             if (PRE) {
                 const int k = fwd ? kk0 : nb - 1 - kk0, c0 = k * BR, ks = min(BR, n - c0);
