@@ -97,7 +97,7 @@ RL_API uint64_t rl_launch_count(void);
                                           elimination step ends in a grid barrier over all of them) */
 #define RL_TUNE_TEST_WITHHOLD_CHUNK 100 /* tests only: the host batched path never sets this chunk's arrival
                                            flag, so its wait runs out (RL_ERR_TIMEOUT): [-1, 255], default -1 */
-#define RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK 101 /* tests only: the few-right-hand-side triangular sweep never
+#define RL_TUNE_TEST_WITHHOLD_SWEEP_BLOCK 101 /* tests only: the one-launch triangular sweep never
                                                  publishes this 64-row block: [-1, 2^30], default -1 */
 RL_API rl_status rl_tune_set(int key, int64_t value);
 RL_API rl_status rl_tune_get(int key, int64_t *value);
